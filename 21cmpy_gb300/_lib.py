@@ -1,0 +1,99 @@
+"""ctypes binding of the engine's C ABI (include/es_engine.h).
+
+The library is loaded from the package directory only; there is no fallback: if it is missing
+or fails to load, every engine call raises :class:`EngineUnavailable`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libes_engine.so"
+
+ES_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "unsupported box size"}
+
+
+class EngineUnavailable(RuntimeError):
+    """The compiled CUDA engine is not built or cannot be loaded."""
+
+
+class EngineError(RuntimeError):
+    """A C-ABI call returned a failure code."""
+
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed ({ERRORS.get(code, code)}): {msg}")
+        self.code = code
+
+
+class es_radius(C.Structure):
+    _fields_ = [("R", C.c_float), ("denom", C.c_float)]
+
+
+class es_ionize_params(C.Structure):
+    _fields_ = [
+        ("n_radii", C.c_int), ("radii", C.POINTER(es_radius)),
+        ("delta_c", C.c_float), ("fc_mean_ps", C.c_float), ("zeta", C.c_float),
+        ("growth_scale", C.c_float), ("normalize_mean", C.c_int), ("filter_type", C.c_int),
+        ("update", C.c_int), ("ref_compat", C.c_int), ("output", C.c_int),
+    ]
+
+
+_PROTOS = {
+    "es_plan_create": (C.c_int, [C.c_int, C.c_double, C.c_int, C.POINTER(C.c_void_p)]),
+    "es_plan_destroy": (C.c_int, [C.c_void_p]),
+    "es_plan_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int]),
+    "es_supported_sizes": (C.c_int, [C.POINTER(C.c_int), C.c_int]),
+    "es_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "es_ionize": (C.c_int, [C.c_void_p, C.POINTER(es_ionize_params), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "es_delta_T": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "es_power_spectrum": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_int,
+                                    C.c_void_p, C.c_void_p]),
+    "es_fft_r2c": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "es_fft_c2r": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
+    "es_version": (C.c_int, []),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def exported_symbols() -> list:
+    return sorted(_PROTOS)
+
+
+def load(path: Path | None = None):
+    """Load libes_engine.so and declare its prototypes (idempotent)."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path is not None else LIB_PATH
+        if not p.exists():
+            raise EngineUnavailable(f"{p} is not built; run __graft_entry__.build() (nvcc, sm_103a)")
+        try:
+            lib = C.CDLL(str(p))
+        except OSError as e:
+            raise EngineUnavailable(f"cannot load {p}: {e}") from e
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def last_error(lib=None) -> str:
+    lib = lib or load()
+    buf = C.create_string_buffer(1024)
+    lib.es_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(fn: str, code: int, lib=None):
+    if code != ES_OK:
+        raise EngineError(fn, code, last_error(lib))

@@ -1,0 +1,628 @@
+// Host engine and C ABI of the excursion-set path (declared in include/es_engine.h), plus the
+// size-independent kernels: filter tables, final partial ionisation, sphere painting, delta_T
+// and layout conversions for the FFT self-tests.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "es_engine.h"
+#include "es_kernels.cuh"
+#include "es_ops.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define ES_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t err__ = (call);                                                         \
+    if (err__ != cudaSuccess)                                                           \
+      return fail(ES_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(err__));         \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) err = cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+typedef cudaError_t (*launch_fn)(int, const es::OpArgs*, cudaStream_t);
+typedef void (*geom_fn)(es::OpGeometry*);
+
+struct SizeEntry { int n; launch_fn launch; geom_fn geom; };
+#define ES_SIZE_ENTRY(N) {N, es_launch_##N, es_geometry_##N},
+const SizeEntry kSizes[] = {ES_FOR_EACH_SIZE(ES_SIZE_ENTRY)};
+#undef ES_SIZE_ENTRY
+
+const SizeEntry* find_size(int n) {
+  for (const auto& s : kSizes)
+    if (s.n == n) return &s;
+  return nullptr;
+}
+
+}  // namespace
+
+// per-radius constants derived on the host in double precision
+struct RadDev {
+  float R;
+  float denom;
+  int k2cut;      // largest integer k^2 kept by the k-space top-hat (INT_MAX: no cut)
+  int r2max;      // largest integer squared cell distance painted by a sphere (-1: none)
+};
+
+struct es_plan {
+  int n = 0, m = 0, device = 0, sms = 0, max_radii = 0, k2n = 0;
+  double box_len = 0;
+  float dk = 0;
+  const SizeEntry* size = nullptr;
+  es::OpGeometry geo{};
+  // workspace
+  void* base = nullptr;
+  size_t bytes = 0;
+  float2 *X = nullptr, *Xnyq = nullptr, *T = nullptr, *Tnyq = nullptr, *tw = nullptr;
+  float* dR[2] = {nullptr, nullptr};
+  uint32_t* flags = nullptr;
+  uint32_t* centers = nullptr;
+  float* wtab = nullptr;
+  float* partials = nullptr;
+  unsigned* counters = nullptr;     // [0] reductions, [1] centre count
+  float* stats = nullptr;           // [max_radii + 2][4]
+  RadDev* rad = nullptr;
+  int* thr = nullptr;
+  // pinned host staging for per-call parameter uploads
+  RadDev* h_rad = nullptr;
+  int* h_thr = nullptr;
+  cudaEvent_t staged = nullptr;     // last upload from the staging buffers
+  size_t partial_floats = 0;
+};
+
+namespace {
+
+constexpr int kStatsStride = 4;
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct Layout {
+  size_t X, Xnyq, T, Tnyq, tw, dR0, dR1, flags, centers, wtab, partials, counters, stats, rad, thr, total;
+};
+
+Layout layout(int n, int max_radii, size_t partial_floats) {
+  const size_t N = n, M = n / 2;
+  const size_t k2n = 3 * M * M + 1;
+  Layout L{};
+  size_t off = 0;
+  auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+  L.X = take(N * N * M * 8);
+  L.Xnyq = take(N * N * 8);
+  L.T = take(N * N * M * 8);
+  L.Tnyq = take(N * N * 8);
+  L.tw = take(N * 8);
+  L.dR0 = take(N * N * N * 4);
+  L.dR1 = take(N * N * N * 4);
+  L.flags = take(N * N * N / 8);
+  L.centers = take(N * N * N * 4);
+  L.wtab = take((size_t)max_radii * k2n * 4);
+  L.partials = take(partial_floats * 4);
+  L.counters = take(64);
+  L.stats = take((size_t)(max_radii + 2) * kStatsStride * 4);
+  L.rad = take((size_t)max_radii * sizeof(RadDev));
+  L.thr = take(es::PK_MAX_BINS * 4);
+  L.total = off;
+  return L;
+}
+
+int occupancy_grid(const es_plan* p, int tiles, int threads, int smem) {
+  // resident CTAs per SM from the thread and shared-memory budgets of sm_103a
+  int by_threads = 2048 / threads;
+  int by_smem = (227 * 1024) / (smem + 1024);
+  int per_sm = by_threads < by_smem ? by_threads : by_smem;
+  if (per_sm < 1) per_sm = 1;
+  long g = (long)p->sms * per_sm;
+  return (int)(tiles < g ? tiles : g);
+}
+
+size_t partial_floats_for(int sms, const es::OpGeometry& g) {
+  size_t row = (size_t)sms * 16, col = (size_t)sms * 16;
+  size_t pk = col * 3 * es::PK_MAX_BINS;
+  size_t el = (size_t)sms * 16;
+  size_t m = row > pk ? row : pk;
+  return m > el ? m : el;
+}
+
+// ------------------------------------------------------------------ size-independent kernels
+
+__device__ __forceinline__ float rtophat_f(float x) {
+  // W(x) = 3 (sin x - x cos x) / x^3; its Taylor series sum_n 3 (-1)^n (2n+2) x^(2n) / (2n+3)!
+  // below x = 1 avoids the cancellation of the closed form
+  if (x < 1.0f) {
+    const float y = x * x;
+    return 1.0f + y * (-0.1f + y * (1.0f / 280.0f + y * (-1.0f / 15120.0f +
+           y * (1.0f / 1330560.0f + y * (-1.0f / 172972800.0f)))));
+  }
+  float s, c;
+  sincosf(x, &s, &c);
+  return 3.0f * (s - x * c) / (x * x * x);
+}
+
+__global__ void filter_table_kernel(float* wtab, int k2n, const RadDev* rad, int nr, float dk,
+                                    int filter, int ref_compat, float inv_n3) {
+  const long total = (long)nr * k2n;
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(idx / k2n), k2 = (int)(idx % k2n);
+    const RadDev rd = rad[r];
+    const float kR = dk * sqrtf((float)k2) * rd.R;
+    float W;
+    if (!ref_compat) {
+      if (filter == 0) W = rtophat_f(kR);
+      else if (filter == 1) W = k2 <= rd.k2cut ? 1.0f : 0.0f;
+      else { const float x = 0.643f * kR; W = expf(-0.5f * x * x); }
+    } else {   // find_bubbles.cu:28-41, switch without break
+      W = 1.0f;
+      float x = kR;
+      if (filter == 0 && kR > 1e-4f) W = rtophat_f(kR);
+      if (filter <= 1) { x *= 0.413566994f; if (k2 > rd.k2cut) W = 0.0f; }
+      x *= 0.643f;
+      W *= expf(-0.5f * x * x);
+    }
+    wtab[idx] = W * inv_n3;
+  }
+}
+
+template <int T>
+__global__ void __launch_bounds__(T) final_kernel(const float2* dR, const uint32_t* flags, long pairs,
+                                                  float dc, float denom, const float* stats,
+                                                  float zeta, float inv_zeta, int output,
+                                                  float2* out, float* partials, unsigned* counter,
+                                                  float* nf, float inv_n3) {
+  __shared__ float sred[T / 32];
+  const float norm = stats[2];
+  float acc = 0.f;
+  for (long p = blockIdx.x * (long)T + threadIdx.x; p < pairs; p += (long)gridDim.x * T) {
+    const float2 d = dR[p];
+    const uint32_t w = __ldg(flags + (p * 2) / 32);
+    const int bit = (int)((p * 2) % 32);
+    float ion[2];
+    const float dv[2] = {d.x, d.y};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if ((w >> (bit + h)) & 1u) { ion[h] = 1.0f; continue; }
+      const float f = erfcf((dc - dv[h]) / denom) * norm;
+      ion[h] = f >= inv_zeta ? 1.0f : f * zeta;        // final_kernel (find_bubbles.cu:150-157)
+    }
+    acc += (1.0f - ion[0]) + (1.0f - ion[1]);
+    out[p] = output == 0 ? make_float2(1.0f - ion[0], 1.0f - ion[1]) : make_float2(ion[0], ion[1]);
+  }
+  float total;
+  if (es::grid_sum<T>(acc, partials, counter, sred, &total) && threadIdx.x == 0) *nf = total * inv_n3;
+}
+
+template <int T>
+__global__ void __launch_bounds__(T) delta_T_kernel(const float2* xH, const float2* delta, long pairs,
+                                                    float c, float2* dT, float* partials,
+                                                    unsigned* counter, float* ave, float inv_n3) {
+  __shared__ float sred[T / 32];
+  float acc = 0.f;
+  for (long p = blockIdx.x * (long)T + threadIdx.x; p < pairs; p += (long)gridDim.x * T) {
+    const float2 x = xH[p], d = delta[p];
+    const float2 t = make_float2(c * x.x * (1.0f + d.x), c * x.y * (1.0f + d.y));  // delta_T.py:75
+    acc += t.x + t.y;
+    dT[p] = t;
+  }
+  float total;
+  if (es::grid_sum<T>(acc, partials, counter, sred, &total) && threadIdx.x == 0) *ave = total * inv_n3;
+}
+
+__device__ __forceinline__ int isqrt_dev(int v) {
+  int r = (int)sqrtf((float)v);
+  while (r * r > v) --r;
+  while ((r + 1) * (r + 1) <= v) ++r;
+  return r;
+}
+
+__device__ __forceinline__ void set_bits(uint32_t* flags, long a, long b) {
+  // set bits a..b (inclusive) of the flag bitmap
+  for (long w = a / 32; w <= b / 32; ++w) {
+    const int lo = (int)((a > w * 32 ? a : w * 32) - w * 32);
+    const int hi = (int)((b < w * 32 + 31 ? b : w * 32 + 31) - w * 32);
+    const uint32_t himask = hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u);
+    atomicOr(flags + w, himask & ~((1u << lo) - 1u));
+  }
+}
+
+// update_sphere_kernel (find_bubbles.cu:73-102): every cell within |d|^2 <= r2max of a centre
+// is ionised.  One warp per centre; lanes split the (dz, dy) rows of the ball.
+__global__ void paint_kernel(const uint32_t* centers, const unsigned* count, uint32_t* flags, int n,
+                             int r2max, int periodic) {
+  const unsigned cnt = *count;
+  if (r2max < 0) return;
+  const int lane = threadIdx.x & 31;
+  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+  const int r = isqrt_dev(r2max), side = 2 * r + 1;
+  for (long ci = warp; ci < (long)cnt; ci += nwarps) {
+    const uint32_t v = centers[ci];
+    const int cx = (int)(v % n), cy = (int)((v / n) % n), cz = (int)(v / ((uint32_t)n * n));
+    for (int idx = lane; idx < side * side; idx += 32) {
+      const int dz = idx / side - r, dy = idx % side - r;
+      const int rem = r2max - dz * dz - dy * dy;
+      if (rem < 0) continue;
+      const int w = isqrt_dev(rem);
+      int z = cz + dz, y = cy + dy;
+      if (periodic) { z = ((z % n) + n) % n; y = ((y % n) + n) % n; }
+      else if (z < 0 || z >= n || y < 0 || y >= n) continue;
+      const long rb = ((long)z * n + y) * n;
+      int x0 = cx - w, x1 = cx + w;
+      if (periodic) {
+        if (x1 - x0 + 1 >= n) { set_bits(flags, rb, rb + n - 1); continue; }
+        if (x0 < 0) { set_bits(flags, rb + x0 + n, rb + n - 1); x0 = 0; }
+        if (x1 >= n) { set_bits(flags, rb, rb + x1 - n); x1 = n - 1; }
+      } else {
+        if (x0 < 0) x0 = 0;
+        if (x1 > n - 1) x1 = n - 1;
+      }
+      set_bits(flags, rb + x0, rb + x1);
+    }
+  }
+}
+
+// numpy rfftn layout (n, n, n/2+1)  <->  main (n, n, n/2) + nyq (n, n)
+__global__ void to_std_kernel(const float2* mainp, const float2* nyq, float2* out, int n) {
+  const int m = n / 2;
+  const long total = (long)n * n * (m + 1);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long row = i / (m + 1);
+    const int x = (int)(i % (m + 1));
+    out[i] = x < m ? mainp[row * m + x] : nyq[row];
+  }
+}
+
+__global__ void from_std_kernel(const float2* in, float2* mainp, float2* nyq, int n) {
+  const int m = n / 2;
+  const long total = (long)n * n * (m + 1);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long row = i / (m + 1);
+    const int x = (int)(i % (m + 1));
+    if (x < m) mainp[row * m + x] = in[i]; else nyq[row] = in[i];
+  }
+}
+
+es::OpArgs base_args(const es_plan* p) {
+  es::OpArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.tw = p->tw;
+  a.partials = p->partials;
+  a.counter = p->counters;
+  a.scale = 1.0f;
+  return a;
+}
+
+int run_op(const es_plan* p, int op, es::OpArgs a, int grid, cudaStream_t s) {
+  a.grid = grid;
+  cudaError_t e = p->size->launch(op, &a, s);
+  if (e != cudaSuccess) return fail(ES_E_CUDA, "kernel op %d (n=%d) launch failed: %s", op, p->n, cudaGetErrorString(e));
+  return ES_OK;
+}
+
+int grid_col_z(const es_plan* p, bool pk) {
+  return occupancy_grid(p, p->geo.col_tiles_z, p->geo.col_threads, pk ? p->geo.col_smem_pk : p->geo.col_smem);
+}
+int grid_col_y(const es_plan* p) { return occupancy_grid(p, p->geo.col_tiles_y, p->geo.col_threads, p->geo.col_smem); }
+int grid_row(const es_plan* p) { return occupancy_grid(p, p->geo.row_tiles, p->geo.row_threads, p->geo.row_smem); }
+int grid_elem(const es_plan* p) { return p->sms * 8; }
+
+// wait until the previous upload from the staging buffers has been consumed
+int reuse_staging(es_plan* p) {
+  cudaError_t e = cudaEventSynchronize(p->staged);
+  if (e != cudaSuccess) return fail(ES_E_CUDA, "cudaEventSynchronize: %s", cudaGetErrorString(e));
+  return ES_OK;
+}
+
+// forward transform of a real box into (mainp, nyq); rows -> y -> z
+int forward_into(es_plan* p, const float* in, float scale, float2* mainp, float2* nyq, cudaStream_t s) {
+  es::OpArgs a = base_args(p);
+  a.rin = reinterpret_cast<const float2*>(in);
+  a.cout = mainp;
+  a.scale = scale;
+  int rc = run_op(p, es::OP_ROW_R2C_SCALE, a, grid_row(p), s);
+  if (rc) return rc;
+  a = base_args(p);
+  a.cin = mainp; a.cout = mainp; a.cout_nyq = nyq;
+  if ((rc = run_op(p, es::OP_COL_Y_FWD, a, grid_col_y(p), s))) return rc;
+  a = base_args(p);
+  a.cin = mainp; a.cin_nyq = nyq; a.cout = mainp; a.cout_nyq = nyq;
+  return run_op(p, es::OP_COL_Z_FWD, a, grid_col_z(p, false), s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int es_version(void) { return 1; }
+
+int es_last_error(char* buf, int len) {
+  if (!buf || len <= 0) return ES_E_ARG;
+  std::snprintf(buf, (size_t)len, "%s", g_last_error.c_str());
+  return ES_OK;
+}
+
+int es_supported_sizes(int* sizes, int cap) {
+  int c = 0;
+  for (const auto& s : kSizes) {
+    if (sizes && c < cap) sizes[c] = s.n;
+    ++c;
+  }
+  return c;
+}
+
+size_t es_plan_workspace_bytes(int n, int max_radii) {
+  const SizeEntry* se = find_size(n);
+  if (!se || max_radii <= 0) return 0;
+  es::OpGeometry g{};
+  se->geom(&g);
+  // partial-sum space is sized for the largest GB300 part (152 SMs) when no device is queried
+  return layout(n, max_radii, partial_floats_for(152, g)).total;
+}
+
+int es_plan_create(int n, double box_len, int max_radii, es_plan** out) {
+  if (!out) return fail(ES_E_ARG, "es_plan_create: plan pointer is NULL");
+  *out = nullptr;
+  const SizeEntry* se = find_size(n);
+  if (!se) return fail(ES_E_UNSUPPORTED, "es_plan_create: HII_DIM=%d has no compiled kernels", n);
+  if (!(box_len > 0)) return fail(ES_E_ARG, "es_plan_create: BOX_LEN must be positive");
+  if (max_radii <= 0 || max_radii > 4096) return fail(ES_E_ARG, "es_plan_create: max_radii out of range");
+  es_plan* p = new es_plan();
+  p->n = n; p->m = n / 2; p->box_len = box_len; p->max_radii = max_radii; p->size = se;
+  p->k2n = 3 * p->m * p->m + 1;
+  // DELTA_K = float32(2 pi / float32(BOX_LEN)) (delta_T.py:52)
+  p->dk = (float)(2.0 * M_PI / (double)(float)box_len);
+  se->geom(&p->geo);
+  auto cleanup = [&](int code) { es_plan_destroy(p); return code; };
+  if (cudaGetDevice(&p->device) != cudaSuccess) return cleanup(fail(ES_E_CUDA, "no CUDA device"));
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, p->device) != cudaSuccess) return cleanup(fail(ES_E_CUDA, "cudaGetDeviceProperties failed"));
+  p->sms = prop.multiProcessorCount;
+  p->partial_floats = partial_floats_for(p->sms, p->geo);
+  Layout L = layout(n, max_radii, p->partial_floats);
+  if (cudaMalloc(&p->base, L.total) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(fail(ES_E_NOMEM, "es_plan_create: cannot allocate %zu bytes of workspace", L.total));
+  }
+  p->bytes = L.total;
+  char* b = static_cast<char*>(p->base);
+  p->X = (float2*)(b + L.X); p->Xnyq = (float2*)(b + L.Xnyq);
+  p->T = (float2*)(b + L.T); p->Tnyq = (float2*)(b + L.Tnyq);
+  p->tw = (float2*)(b + L.tw);
+  p->dR[0] = (float*)(b + L.dR0); p->dR[1] = (float*)(b + L.dR1);
+  p->flags = (uint32_t*)(b + L.flags);
+  p->centers = (uint32_t*)(b + L.centers);
+  p->wtab = (float*)(b + L.wtab);
+  p->partials = (float*)(b + L.partials);
+  p->counters = (unsigned*)(b + L.counters);
+  p->stats = (float*)(b + L.stats);
+  p->rad = (RadDev*)(b + L.rad);
+  p->thr = (int*)(b + L.thr);
+  if (cudaMallocHost(&p->h_rad, sizeof(RadDev) * max_radii) != cudaSuccess ||
+      cudaMallocHost(&p->h_thr, sizeof(int) * es::PK_MAX_BINS) != cudaSuccess)
+    return cleanup(fail(ES_E_NOMEM, "es_plan_create: pinned staging allocation failed"));
+  if (cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming) != cudaSuccess)
+    return cleanup(fail(ES_E_CUDA, "es_plan_create: cudaEventCreate failed"));
+  // twiddles w_n^m = exp(-2 pi i m / n) in double, rounded once
+  std::vector<float2> tw(n);
+  for (int m = 0; m < n; ++m) {
+    const double ang = -2.0 * M_PI * (double)m / (double)n;
+    tw[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+  }
+  if (cudaMemcpy(p->tw, tw.data(), n * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(p->counters, 0, 64) != cudaSuccess || cudaMemset(p->stats, 0, (size_t)(max_radii + 2) * kStatsStride * 4) != cudaSuccess)
+    return cleanup(fail(ES_E_CUDA, "es_plan_create: initial upload failed"));
+  if (cudaEventRecord(p->staged, 0) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
+    return cleanup(fail(ES_E_CUDA, "es_plan_create: synchronisation failed"));
+  *out = p;
+  return ES_OK;
+}
+
+int es_plan_destroy(es_plan* p) {
+  if (!p) return ES_OK;
+  DeviceGuard g(p->device);
+  if (p->staged) cudaEventSynchronize(p->staged);
+  if (p->base) cudaFree(p->base);
+  if (p->h_rad) cudaFreeHost(p->h_rad);
+  if (p->h_thr) cudaFreeHost(p->h_thr);
+  if (p->staged) cudaEventDestroy(p->staged);
+  delete p;
+  return ES_OK;
+}
+
+int es_forward(es_plan* p, const float* delta, void* stream) {
+  if (!p || !delta) return fail(ES_E_ARG, "es_forward: NULL argument");
+  DeviceGuard g(p->device);
+  return forward_into(p, delta, 1.0f, p->X, p->Xnyq, (cudaStream_t)stream);
+}
+
+int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, void* stream) {
+  if (!p || !prm || !out || !nf) return fail(ES_E_ARG, "es_ionize: NULL argument");
+  const int nr = prm->n_radii;
+  if (nr < 1 || nr > p->max_radii || !prm->radii)
+    return fail(ES_E_ARG, "es_ionize: n_radii=%d outside [1, %d]", nr, p->max_radii);
+  if (prm->filter_type < 0 || prm->filter_type > 2) return fail(ES_E_ARG, "es_ionize: filter_type must be 0, 1 or 2");
+  if (prm->update < 0 || prm->update > 1) return fail(ES_E_ARG, "es_ionize: update must be 0 or 1");
+  if (!(prm->zeta > 0)) return fail(ES_E_ARG, "es_ionize: zeta must be positive");
+  for (int r = 0; r < nr; ++r)
+    if (!(prm->radii[r].R > 0) || !(prm->radii[r].denom > 0) || !std::isfinite(prm->radii[r].denom))
+      return fail(ES_E_ARG, "es_ionize: radius %d has R=%g denom=%g", r, prm->radii[r].R, prm->radii[r].denom);
+  DeviceGuard g(p->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = reuse_staging(p);
+  if (rc) return rc;
+  const double scale = p->box_len / p->n;
+  for (int r = 0; r < nr; ++r) {
+    RadDev rd;
+    rd.R = prm->radii[r].R;
+    rd.denom = prm->radii[r].denom;
+    // k-space top-hat keeps modes with (dk |k| R) * 0.413566994 <= 1 (find_bubbles.cu:34-37)
+    rd.k2cut = 0x7fffffff;
+    if (prm->filter_type == 1 || (prm->ref_compat && prm->filter_type == 0)) {
+      const double R = rd.R, dk = p->dk;
+      long m = (long)std::floor(std::pow(1.0 / (0.413566994 * dk * R), 2)) + 2;
+      while (m >= 0 && (dk * std::sqrt((double)m) * R) * 0.413566994 > 1.0) --m;
+      rd.k2cut = (int)(m < p->k2n ? m : p->k2n);
+    }
+    // sphere: cells with integer |d|^2 < R_cells^2 (find_bubbles.cu:97-98)
+    if (prm->ref_compat) {
+      const float r2 = rd.R * rd.R;                  // R in Mpc used as cells, float32 compare
+      long m = (long)std::floor((double)r2);
+      while (m >= 0 && (float)m >= r2) --m;
+      rd.r2max = (int)m;
+    } else {
+      const double rc2 = std::pow((double)rd.R / scale, 2);
+      long m = (long)std::floor(rc2);
+      while (m >= 0 && (double)m >= rc2) --m;
+      rd.r2max = (int)m;
+    }
+    p->h_rad[r] = rd;
+  }
+  ES_CUDA(cudaMemcpyAsync(p->rad, p->h_rad, sizeof(RadDev) * nr, cudaMemcpyHostToDevice, s));
+  ES_CUDA(cudaEventRecord(p->staged, s));
+  const float inv_n3 = (float)(1.0 / ((double)p->n * p->n * p->n));
+  filter_table_kernel<<<p->sms * 4, 256, 0, s>>>(p->wtab, p->k2n, p->rad, nr, p->dk, prm->filter_type,
+                                                   prm->ref_compat, inv_n3);
+  ES_CUDA(cudaGetLastError());
+  const size_t N3 = (size_t)p->n * p->n * p->n;
+  ES_CUDA(cudaMemsetAsync(p->flags, 0, N3 / 8, s));
+  const float inv_zeta = (float)(1.0 / (double)prm->zeta);
+  for (int r = 0; r < nr; ++r) {
+    es::OpArgs a = base_args(p);
+    a.cin = p->X; a.cin_nyq = p->Xnyq; a.cout = p->T; a.cout_nyq = p->Tnyq;
+    a.wtab = p->wtab + (size_t)r * p->k2n;
+    a.scale = prm->growth_scale;
+    if ((rc = run_op(p, es::OP_COL_Z_INV_FILTER, a, grid_col_z(p, false), s))) return rc;
+    a = base_args(p);
+    a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T;
+    if ((rc = run_op(p, es::OP_COL_Y_INV, a, grid_col_y(p), s))) return rc;
+    if (prm->update == 1 && r > 0) ES_CUDA(cudaMemsetAsync(p->counters + 1, 0, sizeof(unsigned), s));
+    a = base_args(p);
+    a.cin = p->T;
+    a.rout = reinterpret_cast<float2*>(p->dR[r & 1]);
+    a.prev = reinterpret_cast<const float2*>(p->dR[(r + 1) & 1]);
+    a.has_prev = r > 0;
+    a.flags = p->flags;
+    a.dc = prm->delta_c;
+    a.denom = prm->radii[r].denom;
+    a.denom_prev = r > 0 ? prm->radii[r - 1].denom : 1.0f;
+    a.stats_prev = p->stats + (size_t)(r > 0 ? r - 1 : 0) * kStatsStride;
+    a.stats_out = p->stats + (size_t)r * kStatsStride;
+    a.inv_zeta = inv_zeta;
+    a.update = prm->update;
+    a.centers = p->centers;
+    a.center_count = p->counters + 1;
+    a.fc_mean = prm->fc_mean_ps;
+    a.normalize = prm->normalize_mean;
+    if ((rc = run_op(p, es::OP_ROW_C2R_IONIZE, a, grid_row(p), s))) return rc;
+    if (prm->update == 1 && r > 0) {
+      paint_kernel<<<p->sms * 4, 256, 0, s>>>(p->centers, p->counters + 1, p->flags, p->n,
+                                              p->h_rad[r - 1].r2max, prm->ref_compat ? 0 : 1);
+      ES_CUDA(cudaGetLastError());
+    }
+  }
+  final_kernel<256><<<grid_elem(p), 256, 0, s>>>(
+      reinterpret_cast<const float2*>(p->dR[(nr - 1) & 1]), p->flags, (long)(N3 / 2), prm->delta_c,
+      prm->radii[nr - 1].denom, p->stats + (size_t)(nr - 1) * kStatsStride, prm->zeta, inv_zeta,
+      prm->output, reinterpret_cast<float2*>(out), p->partials, p->counters, nf, inv_n3);
+  ES_CUDA(cudaGetLastError());
+  return ES_OK;
+}
+
+int es_delta_T(es_plan* p, const float* xH, const float* delta, float c, float* dT, float* ave, void* stream) {
+  if (!p || !xH || !delta || !dT || !ave) return fail(ES_E_ARG, "es_delta_T: NULL argument");
+  DeviceGuard g(p->device);
+  const size_t N3 = (size_t)p->n * p->n * p->n;
+  delta_T_kernel<256><<<grid_elem(p), 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const float2*>(xH), reinterpret_cast<const float2*>(delta), (long)(N3 / 2), c,
+      reinterpret_cast<float2*>(dT), p->partials, p->counters, ave, (float)(1.0 / (double)N3));
+  ES_CUDA(cudaGetLastError());
+  return ES_OK;
+}
+
+int es_power_spectrum(es_plan* p, const float* dT, const float* ave, const int* thr, int nbins,
+                      int dimensional, float* out, void* stream) {
+  if (!p || !dT || !ave || !thr || !out) return fail(ES_E_ARG, "es_power_spectrum: NULL argument");
+  if (nbins < 1 || nbins > es::PK_MAX_BINS) return fail(ES_E_ARG, "es_power_spectrum: nbins=%d outside [1, %d]", nbins, es::PK_MAX_BINS);
+  for (int b = 1; b < nbins; ++b)
+    if (thr[b] < thr[b - 1]) return fail(ES_E_ARG, "es_power_spectrum: k^2 thresholds must be non-decreasing");
+  DeviceGuard g(p->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = reuse_staging(p);
+  if (rc) return rc;
+  std::memcpy(p->h_thr, thr, sizeof(int) * nbins);
+  ES_CUDA(cudaMemcpyAsync(p->thr, p->h_thr, sizeof(int) * nbins, cudaMemcpyHostToDevice, s));
+  ES_CUDA(cudaEventRecord(p->staged, s));
+  const double L = (double)(float)p->box_len;
+  es::OpArgs a = base_args(p);
+  a.rin = reinterpret_cast<const float2*>(dT);
+  a.cout = p->T;
+  a.ave = ave;
+  a.pk_norm = (float)(L * L * L / ((double)p->n * p->n * p->n));
+  a.dimensional = dimensional;
+  if ((rc = run_op(p, es::OP_ROW_R2C_PK, a, grid_row(p), s))) return rc;
+  a = base_args(p);
+  a.cin = p->T; a.cout = p->T; a.cout_nyq = p->Tnyq;
+  if ((rc = run_op(p, es::OP_COL_Y_FWD, a, grid_col_y(p), s))) return rc;
+  a = base_args(p);
+  a.cin = p->T; a.cin_nyq = p->Tnyq;
+  a.thr = p->thr; a.nbins = nbins; a.dk = p->dk; a.volume = (float)(L * L * L);
+  a.pk_out = out;
+  return run_op(p, es::OP_COL_Z_FWD_PK, a, grid_col_z(p, true), s);
+}
+
+int es_fft_r2c(es_plan* p, const float* in, void* out, void* stream) {
+  if (!p || !in || !out) return fail(ES_E_ARG, "es_fft_r2c: NULL argument");
+  DeviceGuard g(p->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = forward_into(p, in, 1.0f, p->T, p->Tnyq, s);
+  if (rc) return rc;
+  to_std_kernel<<<p->sms * 8, 256, 0, s>>>(p->T, p->Tnyq, (float2*)out, p->n);
+  ES_CUDA(cudaGetLastError());
+  return ES_OK;
+}
+
+int es_fft_c2r(es_plan* p, const void* in, float* out, void* stream) {
+  if (!p || !in || !out) return fail(ES_E_ARG, "es_fft_c2r: NULL argument");
+  DeviceGuard g(p->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  from_std_kernel<<<p->sms * 8, 256, 0, s>>>((const float2*)in, p->T, p->Tnyq, p->n);
+  ES_CUDA(cudaGetLastError());
+  es::OpArgs a = base_args(p);
+  a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T; a.cout_nyq = p->Tnyq;
+  int rc = run_op(p, es::OP_COL_Z_INV, a, grid_col_z(p, false), s);
+  if (rc) return rc;
+  a = base_args(p);
+  a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T;
+  if ((rc = run_op(p, es::OP_COL_Y_INV, a, grid_col_y(p), s))) return rc;
+  a = base_args(p);
+  a.cin = p->T;
+  a.rout = reinterpret_cast<float2*>(out);
+  return run_op(p, es::OP_ROW_C2R_STORE, a, grid_row(p), s);
+}
+
+}  // extern "C"

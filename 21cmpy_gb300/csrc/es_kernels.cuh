@@ -1,0 +1,459 @@
+// Excursion-set engine kernels, templated on the box size N (sm_103a).
+//
+// Spectrum layout in HBM (per box): the half spectrum of an N^3 real box is split into
+//   main[k][j][i], i in [0, N/2)   (N * N * N/2 complex64, rows of N/2 elements)
+//   nyq[k][j]                       (the i = N/2 plane, N * N complex64)
+// where k and j are the z and y wavenumber indices (natural FFT order) and i the x one.
+// Real boxes are C-order [z][y][x] float32, the reference's INDEX(k,j,i) (find_bubbles.cu:6).
+//
+// Passes (each one HBM read + one write of the data it touches):
+//   rows  : length-N real <-> half-complex transform along x (N/2-point complex FFT + split)
+//   col-y : length-N complex FFT along y within each z plane
+//   col-z : length-N complex FFT along z
+// The i = 0 and i = N/2 columns are Hermitian in (j, k); along y they are transformed together
+// as one complex sequence (packed as re + i*im) and split again on the forward side.
+#pragma once
+#include "es_fft.cuh"
+
+namespace es {
+
+enum ColMode { COL_Z_FWD = 0, COL_Y_FWD = 1, COL_Z_INV_FILTER = 2, COL_Y_INV = 3, COL_Z_FWD_PK = 4, COL_Z_INV = 5 };
+enum RowPro { PRO_SCALE = 0, PRO_PK = 1 };
+enum RowEpi { EPI_STORE = 0, EPI_IONIZE = 1 };
+
+constexpr int PK_MAX_BINS = 128;
+
+struct OpArgs {
+  int grid;                       // CTAs to launch (persistent grid-stride)
+  // real boxes viewed as float2 pairs of consecutive x
+  const float2* rin;
+  float2* rout;
+  // spectra
+  const float2* cin;
+  const float2* cin_nyq;
+  float2* cout;
+  float2* cout_nyq;
+  const float2* tw;               // w_N^m = exp(-2 pi i m / N), m < N
+  // row R2C prologue
+  float scale;                    // PRO_SCALE: multiply input by scale
+  const float* ave;               // PRO_PK: device mean of the input
+  float pk_norm;                  // PRO_PK: V / N^3
+  int dimensional;                // PRO_PK: multiply by the mean (DIMENSIONAL_T_POWER_SPEC)
+  // col-z inverse filter (times scale, the growth rescale)
+  const float* wtab;              // W(k^2) / N^3 for this radius
+  // row C2R ionisation epilogue
+  const float2* prev;             // delta_R of the previous radius (pairs)
+  uint32_t* flags;                // ionisation bits, bit v of word v/32
+  int has_prev;
+  float dc;                       // delta_c(z) (float32, find_bubbles.cu:54)
+  float denom;                    // this radius
+  float denom_prev;               // previous radius
+  const float* stats_prev;        // {sum, mean, norm} of the previous radius
+  float inv_zeta;                 // float32(1/zeta)
+  int update;                     // 0 centre pixel, 1 sphere painting
+  uint32_t* centers;              // sphere mode: centres passing at the previous radius
+  unsigned* center_count;
+  // reductions
+  float* partials;
+  unsigned* counter;
+  float* stats_out;               // {sum, mean, norm}
+  float fc_mean;                  // mean collapse fraction (normalisation target)
+  int normalize;                  // rescale fcoll by fc_mean / <fcoll>
+  // P(k)
+  const int* thr;                 // integer k^2 thresholds per bin
+  int nbins;
+  float dk;
+  float volume;
+  float* pk_out;                  // [3 * nbins]: ps_ave, k_ave, count
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum; the result is valid in every thread.  sred holds T/32 floats.
+template <int T>
+__device__ __forceinline__ float block_sum(float v, float* sred) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sred[warp] = v;
+  __syncthreads();
+  float s = 0.f;
+#pragma unroll
+  for (int w = 0; w < T / 32; ++w) s += sred[w];
+  return s;
+}
+
+// Deterministic grid-wide sum: every CTA publishes its partial, the last CTA to arrive adds
+// all partials in a fixed order.  Returns true in the last CTA, with *total set there.
+template <int T>
+__device__ __forceinline__ bool grid_sum(float mine, float* partials, unsigned* counter,
+                                         float* sred, float* total) {
+  __shared__ unsigned s_last;
+  float s = block_sum<T>(mine, sred);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s;
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    s_last = (t == gridDim.x - 1) ? 1u : 0u;
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  float acc = 0.f;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += T) acc += __ldcg(partials + i);
+  acc = block_sum<T>(acc, sred);
+  if (threadIdx.x == 0) *counter = 0u;
+  *total = acc;
+  return true;
+}
+
+template <int N> __device__ __forceinline__ int wrap2(int k) {
+  const int w = (k > N / 2) ? k - N : k;
+  return w * w;
+}
+
+// ------------------------------------------------------------------ column passes (y or z)
+template <int N> struct ColCfg;
+template <> struct ColCfg<32>  { static constexpr int TI = 16, T = 128; };
+template <> struct ColCfg<48>  { static constexpr int TI = 8,  T = 128; };
+template <> struct ColCfg<64>  { static constexpr int TI = 16, T = 128; };
+template <> struct ColCfg<96>  { static constexpr int TI = 16, T = 256; };
+template <> struct ColCfg<128> { static constexpr int TI = 16, T = 256; };
+template <> struct ColCfg<160> { static constexpr int TI = 16, T = 256; };
+template <> struct ColCfg<256> { static constexpr int TI = 16, T = 256; };
+template <> struct ColCfg<512> { static constexpr int TI = 8,  T = 256; };
+
+template <int N, int MODE> struct ColSmem {
+  static constexpr int TI = ColCfg<N>::TI, T = ColCfg<N>::T;
+  static constexpr int fft_bytes = (N + 2 * N * TI) * 8;
+  static constexpr int pk_bytes = (MODE == COL_Z_FWD_PK)
+      ? ((T / 32) * PK_MAX_BINS * 3 + (T / 32) * 32 * 4 + PK_MAX_BINS) * 4 : 0;
+  static constexpr int bytes = fft_bytes + pk_bytes;
+};
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(ColCfg<N>::T) col_pass(OpArgs a) {
+  constexpr int M = N / 2;
+  constexpr int TI = ColCfg<N>::TI, T = ColCfg<N>::T;
+  constexpr bool INV = (MODE == COL_Z_INV_FILTER || MODE == COL_Y_INV || MODE == COL_Z_INV);
+  constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
+  constexpr int CPR = M / TI;
+  static_assert(M % TI == 0 && N % TI == 0, "tile width must divide N/2");
+  const int nmain = N * CPR;
+  const int ntiles = ZPASS ? nmain + N / TI : nmain;
+
+  extern __shared__ float4 smem4[];
+  float2* tw = reinterpret_cast<float2*>(smem4);
+  float2* A = tw + N;
+  float2* B = A + N * TI;
+  float* bins = reinterpret_cast<float*>(B + N * TI);          // [warps][3][PK_MAX_BINS]
+  float* scratch = bins + (T / 32) * PK_MAX_BINS * 3;          // [warps][32][4]
+  int* sthr = reinterpret_cast<int*>(scratch + (T / 32) * 32 * 4);
+  __shared__ float sred[T / 32];
+
+  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
+  if (MODE == COL_Z_FWD_PK) {
+    for (int i = threadIdx.x; i < (T / 32) * PK_MAX_BINS * 3; i += T) bins[i] = 0.f;
+    for (int i = threadIdx.x; i < a.nbins; i += T) sthr[i] = a.thr[i];
+  }
+  __syncthreads();
+
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // ---- addressing of this tile: TI columns, N elements along the transform axis
+    bool nyq_tile = false;
+    int c = 0, plane = 0;
+    size_t off;
+    size_t es_g;
+    if (ZPASS) {
+      if (tile < nmain) { plane = tile / CPR; c = tile % CPR; off = (size_t)plane * M + c * TI; es_g = (size_t)N * M; }
+      else { nyq_tile = true; c = tile - nmain; off = (size_t)c * TI; es_g = N; }
+    } else {
+      plane = tile / CPR; c = tile % CPR; off = (size_t)plane * N * M + c * TI; es_g = M;
+    }
+    const float2* src = nyq_tile ? a.cin_nyq : a.cin;
+    // ---- load (+ filter)
+    for (int e = threadIdx.x; e < N * TI; e += T) {
+      const int row = e / TI, col = e % TI;
+      float2 v = src[off + row * es_g + col];
+      if (MODE == COL_Z_INV_FILTER) {
+        int k2;
+        if (!nyq_tile) { const int kx = c * TI + col; k2 = wrap2<N>(row) + wrap2<N>(plane) + kx * kx; }
+        else { k2 = wrap2<N>(row) + wrap2<N>(c * TI + col) + M * M; }
+        v = cscale(v, __ldg(a.wtab + k2) * a.scale);
+      }
+      A[e] = v;
+    }
+    if (MODE == COL_Y_INV && c == 0) {
+      // pack the Hermitian columns i = 0 and i = N/2: u = y0 + i * yM
+      __syncthreads();
+      for (int j = threadIdx.x; j < N; j += T) {
+        const float2 y0 = A[j * TI];
+        const float2 ym = a.cin_nyq[(size_t)plane * N + j];
+        A[j * TI] = make_float2(y0.x - ym.y, y0.y + ym.x);
+      }
+    }
+    __syncthreads();
+    float2* Rr = fft_lines<N, INV, TI, T, true, TI, 1, N>(A, B, tw);
+
+    if (MODE == COL_Z_FWD_PK) {
+      // ---- spherical binning of k^3 |G|^2 / (2 pi^2 V), |k| and counts, warp-aggregated
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      float* wb = bins + warp * PK_MAX_BINS * 3;
+      float* ws = scratch + warp * 32 * 4;
+      const float inv = 1.0f / (2.0f * 9.8696044010893586f * a.volume);
+      for (int e = threadIdx.x; e < N * TI; e += T) {      // whole warps iterate together
+        const int row = e / TI, col = e % TI;
+        int k2;
+        float wgt;
+        if (!nyq_tile) { const int kx = c * TI + col; k2 = wrap2<N>(row) + wrap2<N>(plane) + kx * kx; wgt = kx == 0 ? 1.f : 2.f; }
+        else { k2 = wrap2<N>(row) + wrap2<N>(c * TI + col) + M * M; wgt = 1.f; }
+        int lo = 0, hi = a.nbins;                           // first bin with k2 <= thr[bin]
+        while (lo < hi) { const int mid = (lo + hi) >> 1; if (k2 <= sthr[mid]) hi = mid; else lo = mid + 1; }
+        int bin = lo;
+        if (k2 == 0) bin = a.nbins;                           // the mean (k = 0) is excluded
+        const float2 g = Rr[e];
+        const float km = a.dk * sqrtf((float)k2);
+        ws[lane * 4 + 0] = wgt * km * km * km * (g.x * g.x + g.y * g.y) * inv;
+        ws[lane * 4 + 1] = wgt * km;
+        ws[lane * 4 + 2] = wgt;
+        const unsigned peers = __match_any_sync(0xffffffffu, bin);
+        __syncwarp();
+        if (bin < a.nbins && lane == __ffs(peers) - 1) {
+          float p = 0.f, k = 0.f, n = 0.f;
+          unsigned m = peers;
+          while (m) {
+            const int l = __ffs(m) - 1;
+            m &= m - 1;
+            p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += ws[l * 4 + 2];
+          }
+          wb[bin] += p; wb[PK_MAX_BINS + bin] += k; wb[2 * PK_MAX_BINS + bin] += n;
+        }
+        __syncwarp();
+      }
+    } else if (MODE == COL_Y_FWD && c == 0) {
+      // split the packed column 0: A = FFT(x0) -> main column 0, B = FFT(xM) -> nyq plane
+      for (int e = threadIdx.x; e < N * TI; e += T) {
+        const int row = e / TI, col = e % TI;
+        if (col == 0) {
+          const float2 v = Rr[row * TI];
+          const float2 w = Rr[((N - row) % N) * TI];
+          a.cout[off + row * es_g] = make_float2(0.5f * (v.x + w.x), 0.5f * (v.y - w.y));
+          a.cout_nyq[(size_t)plane * N + row] = make_float2(0.5f * (v.y + w.y), -0.5f * (v.x - w.x));
+        } else {
+          a.cout[off + row * es_g + col] = Rr[e];
+        }
+      }
+    } else {
+      float2* dst = nyq_tile ? a.cout_nyq : a.cout;
+      for (int e = threadIdx.x; e < N * TI; e += T) {
+        const int row = e / TI, col = e % TI;
+        dst[off + row * es_g + col] = Rr[e];
+      }
+    }
+    __syncthreads();
+  }
+
+  if (MODE == COL_Z_FWD_PK) {
+    // per-CTA bins (fixed warp order) -> partials -> last CTA reduces and writes the averages
+    __syncthreads();
+    const int nb3 = 3 * a.nbins;
+    for (int idx = threadIdx.x; idx < nb3; idx += T) {
+      const int q = idx / a.nbins, bin = idx % a.nbins;
+      float s = 0.f;
+      for (int w = 0; w < T / 32; ++w) s += bins[w * PK_MAX_BINS * 3 + q * PK_MAX_BINS + bin];
+      a.partials[(size_t)blockIdx.x * nb3 + idx] = s;
+    }
+    __shared__ unsigned s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      float* tot = bins;     // reuse: [3 * nbins]
+      for (int idx = threadIdx.x; idx < nb3; idx += T) {
+        float s = 0.f;
+        for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(a.partials + (size_t)b * nb3 + idx);
+        tot[idx] = s;
+      }
+      __syncthreads();
+      for (int bin = threadIdx.x; bin < a.nbins; bin += T) {
+        const float n = tot[2 * a.nbins + bin];
+        a.pk_out[bin] = n > 0.f ? tot[bin] / n : 0.f;                        // ps_ave
+        a.pk_out[a.nbins + bin] = n > 0.f ? tot[a.nbins + bin] / n : 0.f;    // k_ave
+        a.pk_out[2 * a.nbins + bin] = n;                                     // count
+      }
+      if (threadIdx.x == 0) *a.counter = 0u;
+    }
+  }
+  (void)sred;
+}
+
+// ------------------------------------------------------------------ row passes (x)
+template <int N> struct RowCfg;
+template <> struct RowCfg<32>  { static constexpr int RL = 16, T = 128; };
+template <> struct RowCfg<48>  { static constexpr int RL = 8,  T = 128; };
+template <> struct RowCfg<64>  { static constexpr int RL = 8,  T = 128; };
+template <> struct RowCfg<96>  { static constexpr int RL = 8,  T = 128; };
+template <> struct RowCfg<128> { static constexpr int RL = 8,  T = 256; };
+template <> struct RowCfg<160> { static constexpr int RL = 8,  T = 256; };
+template <> struct RowCfg<256> { static constexpr int RL = 8,  T = 256; };
+template <> struct RowCfg<512> { static constexpr int RL = 4,  T = 256; };
+
+template <int N> struct RowSmem {
+  static constexpr int bytes = (N + 2 * RowCfg<N>::RL * (N / 2)) * 8;
+};
+
+// Real rows -> half spectrum rows (main layout; slot 0 holds (X[0], X[N/2]), both real).
+template <int N, int PRO>
+__global__ void __launch_bounds__(RowCfg<N>::T) row_r2c(OpArgs a) {
+  constexpr int M = N / 2, RL = RowCfg<N>::RL, T = RowCfg<N>::T;
+  static_assert((RL * N) % 64 == 0, "row tile must cover whole 64-voxel flag pairs");
+  extern __shared__ float4 smem4[];
+  float2* tw = reinterpret_cast<float2*>(smem4);
+  float2* A = tw + N;
+  float2* B = A + RL * M;
+  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
+  float s = a.scale, sh = 0.f;
+  if (PRO == PRO_PK) {
+    const float ave = *a.ave;
+    // g = (x / ave - 1) V / N^3  (delta_T.py:80-82), optionally times ave
+    s = a.pk_norm / ave;
+    sh = -a.pk_norm;
+    if (a.dimensional) { s *= ave; sh *= ave; }
+  }
+  __syncthreads();
+  const int ntiles = N * N / RL;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const size_t base = (size_t)tile * RL * M;
+    for (int e = threadIdx.x; e < RL * M; e += T) {
+      float2 v = a.rin[base + e];
+      if (PRO == PRO_PK) v = make_float2(fmaf(v.x, s, sh), fmaf(v.y, s, sh));
+      else v = cscale(v, s);
+      A[e] = v;
+    }
+    __syncthreads();
+    float2* Z = fft_lines<M, false, RL, T, false, 1, M, N>(A, B, tw);
+    for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += T) {
+      const int row = q / (M / 2 + 1), m = q % (M / 2 + 1);
+      const float2* z = Z + row * M;
+      float2* out = a.cout + base + (size_t)row * M;
+      if (m == 0) {
+        const float2 z0 = z[0];
+        out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+      } else {
+        const int m2 = M - m;
+        const float2 zm = z[m], zc = z[m2];
+        {
+          const float2 t = cmul(tw[m], make_float2(zm.x - zc.x, zm.y + zc.y));   // w^m (Zm - conj Zc)
+          out[m] = make_float2(0.5f * (zm.x + zc.x + t.y), 0.5f * (zm.y - zc.y - t.x));
+        }
+        if (m2 != m) {
+          const float2 t = cmul(tw[m2], make_float2(zc.x - zm.x, zc.y + zm.y));
+          out[m2] = make_float2(0.5f * (zc.x + zm.x + t.y), 0.5f * (zc.y - zm.y - t.x));
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Half spectrum rows -> real rows, with the excursion-set epilogue.
+template <int N, int EPI>
+__global__ void __launch_bounds__(RowCfg<N>::T) row_c2r(OpArgs a) {
+  constexpr int M = N / 2, RL = RowCfg<N>::RL, T = RowCfg<N>::T;
+  static_assert((RL * N) % 64 == 0, "row tile must cover whole 64-voxel flag pairs");
+  static_assert((RL * M) % 32 == 0 && T % 32 == 0, "whole warps per row tile");
+  extern __shared__ float4 smem4[];
+  float2* tw = reinterpret_cast<float2*>(smem4);
+  float2* A = tw + N;
+  float2* B = A + RL * M;
+  __shared__ float sred[T / 32];
+  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
+  float norm_prev = 1.f, inv_dp = 0.f;
+  if (EPI == EPI_IONIZE && a.has_prev) norm_prev = a.stats_prev[2];
+  const float dc = a.dc, denom = a.denom, dprev = a.denom_prev, izeta = a.inv_zeta;
+  (void)inv_dp;
+  float acc = 0.f;
+  const int lane = threadIdx.x & 31;
+  __syncthreads();
+  const int ntiles = N * N / RL;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const size_t base = (size_t)tile * RL * M;
+    for (int e = threadIdx.x; e < RL * M; e += T) A[e] = a.cin[base + e];
+    __syncthreads();
+    for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += T) {
+      const int row = q / (M / 2 + 1), m = q % (M / 2 + 1);
+      float2* x = A + row * M;
+      if (m == 0) {
+        const float2 x0 = x[0];                       // (X[0], X[N/2]), both real
+        x[0] = make_float2(x0.x + x0.y, x0.x - x0.y);
+      } else {
+        const int m2 = M - m;
+        const float2 xm = x[m], xc = x[m2];
+        // Z[m] = (Xm + conj Xc) + i w^-m (Xm - conj Xc)
+        const float2 t1 = cmul(cconj(tw[m]), make_float2(xm.x - xc.x, xm.y + xc.y));
+        x[m] = make_float2(xm.x + xc.x - t1.y, xm.y - xc.y + t1.x);
+        if (m2 != m) {
+          const float2 t2 = cmul(cconj(tw[m2]), make_float2(xc.x - xm.x, xc.y + xm.y));
+          x[m2] = make_float2(xc.x + xm.x - t2.y, xc.y - xm.y + t2.x);
+        }
+      }
+    }
+    __syncthreads();
+    float2* Zr = fft_lines<M, true, RL, T, false, 1, M, N>(A, B, tw);
+    if (EPI == EPI_STORE) {
+      for (int e = threadIdx.x; e < RL * M; e += T) a.rout[base + e] = Zr[e];
+    } else {
+      for (int e = threadIdx.x; e < RL * M; e += T) {   // whole warps: 64 consecutive voxels
+        const float2 d = Zr[e];
+        acc += erfcf((dc - d.x) / denom) + erfcf((dc - d.y) / denom);
+        if (a.has_prev) {
+          const float2 p = a.prev[base + e];
+          const bool px = erfcf((dc - p.x) / dprev) * norm_prev >= izeta;
+          const bool py = erfcf((dc - p.y) / dprev) * norm_prev >= izeta;
+          const unsigned bx = __ballot_sync(0xffffffffu, px);
+          const unsigned by = __ballot_sync(0xffffffffu, py);
+          if (a.update == 0) {
+            if (lane < 2) {
+              const uint32_t bits = lane == 0
+                  ? (spread16(bx) | (spread16(by) << 1))
+                  : (spread16(bx >> 16) | (spread16(by >> 16) << 1));
+              if (bits) {
+                const size_t w = ((base + e - lane) * 2) / 32 + lane;
+                a.flags[w] |= bits;
+              }
+            }
+          } else if (bx | by) {
+            const unsigned cnt = __popc(bx) + __popc(by);
+            unsigned first = 0;
+            if (lane == 0) first = atomicAdd(a.center_count, cnt);
+            first = __shfl_sync(0xffffffffu, first, 0);
+            const unsigned lt = (1u << lane) - 1u;
+            const unsigned v0 = (unsigned)((base + e) * 2);
+            unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
+            if (px) a.centers[pos++] = v0;
+            if (py) a.centers[pos] = v0 + 1;
+          }
+        }
+        a.rout[base + e] = d;
+      }
+    }
+    __syncthreads();
+  }
+  if (EPI == EPI_IONIZE) {
+    float total;
+    if (grid_sum<T>(acc, a.partials, a.counter, sred, &total) && threadIdx.x == 0) {
+      const float mean = total / ((float)N * (float)N * (float)N);
+      a.stats_out[0] = total;
+      a.stats_out[1] = mean;
+      a.stats_out[2] = a.normalize ? a.fc_mean / mean : 1.f;
+    }
+  }
+}
+
+}  // namespace es

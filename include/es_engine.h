@@ -1,0 +1,103 @@
+/* C ABI of the GB300 excursion-set engine (libes_engine.so).
+ *
+ * Replaces the GPU half of the reference's Programs/find_HII_bubbles.py and Programs/delta_T.py:
+ * plain pointers and sizes, no framework types.  Device pointers are CUDA global-memory
+ * addresses on the device that was current when the plan was created; every call is
+ * asynchronous on the given stream (a cudaStream_t passed as void*, NULL = legacy default
+ * stream).  Return values: 0 on success, a negative ES_E_* code on failure; es_last_error()
+ * returns the message of the calling thread's last failure.
+ *
+ * Layouts: real boxes are C-order float32 [z][y][x] (the reference's INDEX(k,j,i),
+ * find_bubbles.cu:6).  A plan owns its workspace (allocated once in es_plan_create); the
+ * caller owns every input and output buffer.  A plan serves one stream at a time.
+ */
+#ifndef ES_ENGINE_H
+#define ES_ENGINE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ES_OK 0
+#define ES_E_ARG (-1)        /* invalid argument (size, pointer, parameter) */
+#define ES_E_CUDA (-2)       /* a CUDA runtime call failed */
+#define ES_E_NOMEM (-3)      /* workspace allocation failed */
+#define ES_E_UNSUPPORTED (-4) /* box size without compiled kernels */
+
+typedef struct es_plan es_plan;
+
+/* One radius of the descending excursion-set schedule (find_HII_bubbles.py:121-128):
+ * R [Mpc] and denom = sqrt(2 (sigma_min^2 - sigma^2(R))), both as the reference's float32. */
+typedef struct es_radius {
+  float R;
+  float denom;
+} es_radius;
+
+/* Scalars of one ionisation run; the reference pastes DELTAC/ZETA into its kernel source
+ * (find_HII_bubbles.py:63-70) and passes R/denom per launch (l.147-175). */
+typedef struct es_ionize_params {
+  int n_radii;              /* radii in radii[]; the last one is the final radius */
+  const es_radius* radii;   /* host array, descending R */
+  float delta_c;            /* 1.686 / D(z) */
+  float fc_mean_ps;         /* mean collapse fraction erfc(delta_c / (sqrt2 sigma_min)) */
+  float zeta;               /* ionising efficiency ZETA */
+  float growth_scale;       /* density multiplier before filtering (1/D(z) when LE is false) */
+  int normalize_mean;       /* 1: fcoll *= fc_mean_ps / <fcoll> (reference LE == False) */
+  int filter_type;          /* 0 real-space top-hat, 1 k-space top-hat, 2 Gaussian */
+  int update;               /* 0 centre pixel, 1 sphere painting */
+  int ref_compat;           /* 1: reference quirks: filter switch fall-through, sphere radius in
+                               Mpc used as cells, spheres clamped at the box edge */
+  int output;               /* 0: write x_HI = 1 - ionised; 1: write the ionised fraction */
+} es_ionize_params;
+
+/* Replaces the per-box set-up of conv_bubbles (find_HII_bubbles.py:76-91): pyfft Plan, device
+ * boxes.  n: HII_DIM (32, 48, 64, 96, 128, 160, 256 or 512); box_len: BOX_LEN [Mpc];
+ * max_radii: longest schedule the plan will run. */
+int es_plan_create(int n, double box_len, int max_radii, es_plan** plan);
+int es_plan_destroy(es_plan* plan);
+/* Device bytes es_plan_create allocates for (n, max_radii); 0 for an unsupported n. */
+size_t es_plan_workspace_bytes(int n, int max_radii);
+/* Box sizes with compiled kernels, written to sizes[0..cap); returns their count. */
+int es_supported_sizes(int* sizes, int cap);
+
+/* Forward transform of the density box, once per box (the reference repeats it per radius,
+ * find_HII_bubbles.py:141-144).  delta: device float32 n^3. */
+int es_forward(es_plan* plan, const float* delta, void* stream);
+
+/* The radius loop of conv_bubbles (find_HII_bubbles.py:121-192) on the spectrum of the last
+ * es_forward: filter (HII_filter, find_bubbles.cu:12-42), inverse transform, erfc collapse
+ * fraction (fcoll_kernel, cu:43-58), mean normalisation (l.158-160), centre / sphere updates
+ * (update_kernel / update_sphere_kernel, cu:59-140) and the final partial ionisation
+ * (final_kernel, cu:142-158).  out: device float32 n^3; nf: device float, mean of x_HI
+ * (the nf of the output file name, find_HII_bubbles.py:225). */
+int es_ionize(es_plan* plan, const es_ionize_params* params, float* out, float* nf, void* stream);
+
+/* delta_T = const_factor * x_HI * (1 + delta) [mK] and its mean (delta_T.py:73-76).
+ * xH, delta, dT: device float32 n^3; ave: device float. */
+int es_delta_T(es_plan* plan, const float* xH, const float* delta, float const_factor,
+               float* dT, float* ave, void* stream);
+
+/* Spherically binned power spectrum of g = (dT / ave - 1) V / n^3 (times ave when
+ * dimensional), the intended pbox_kernel (delta_T.cu:5-29, delta_T.py:80-98).
+ * k2_thresholds: host int[nbins], a mode of integer |k/dk|^2 = m goes to the first bin b
+ * with m <= k2_thresholds[b]; the k = 0 mode is excluded.  out: device float[3 * nbins] =
+ * per-bin mean of k^3 |g_k|^2 / (2 pi^2 V), mean |k|, and mode count.  nbins <= 128. */
+int es_power_spectrum(es_plan* plan, const float* dT, const float* ave, const int* k2_thresholds,
+                      int nbins, int dimensional, float* out, void* stream);
+
+/* Plain 3-D transforms in numpy's rfftn layout (n, n, n/2 + 1), for testing the FFT passes:
+ * forward unnormalised; inverse unnormalised (numpy irfftn times n^3).  Use the plan's
+ * scratch spectrum, so they invalidate the last es_forward. */
+int es_fft_r2c(es_plan* plan, const float* in, void* out_half, void* stream);
+int es_fft_c2r(es_plan* plan, const void* in_half, float* out, void* stream);
+
+/* Message of the calling thread's last failure, copied into buf (NUL-terminated). */
+int es_last_error(char* buf, int len);
+int es_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ES_ENGINE_H */

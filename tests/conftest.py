@@ -1,0 +1,22 @@
+import importlib
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built engine")
+
+
+@pytest.fixture(scope="session")
+def pkg():
+    return importlib.import_module("21cmpy_gb300")
+
+
+def module(name):
+    return importlib.import_module("21cmpy_gb300." + name)
