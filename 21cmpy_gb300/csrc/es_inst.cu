@@ -9,19 +9,21 @@
 
 namespace es {
 
-template <typename K>
-static cudaError_t launch(K kernel, int smem, const OpArgs& a, int threads, cudaStream_t s) {
-  static unsigned configured = 0u;   // opt-in shared memory above 48 KB, once per kernel and device
+// One static flag per kernel (the template argument is the kernel itself): opt in to more than
+// 48 KB of dynamic shared memory once per kernel and device.
+template <auto Kernel>
+static cudaError_t launch(int smem, const OpArgs& a, int threads, cudaStream_t s) {
+  static unsigned configured = 0u;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   const unsigned bit = 1u << (dev & 31);
   if (!(configured & bit)) {
-    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     configured |= bit;
   }
-  kernel<<<a.grid, threads, smem, s>>>(a);
+  Kernel<<<a.grid, threads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -29,25 +31,25 @@ template <int N>
 static cudaError_t launch_op(int op, const OpArgs& a, cudaStream_t s) {
   switch (op) {
     case OP_COL_Z_FWD:
-      return launch(col_pass<N, COL_Z_FWD>, ColSmem<N, COL_Z_FWD>::bytes, a, ColCfg<N>::T, s);
+      return launch<col_pass<N, COL_Z_FWD>>(ColSmem<N, COL_Z_FWD>::bytes, a, ColCfg<N>::T, s);
     case OP_COL_Y_FWD:
-      return launch(col_pass<N, COL_Y_FWD>, ColSmem<N, COL_Y_FWD>::bytes, a, ColCfg<N>::T, s);
+      return launch<col_pass<N, COL_Y_FWD>>(ColSmem<N, COL_Y_FWD>::bytes, a, ColCfg<N>::T, s);
     case OP_COL_Z_INV_FILTER:
-      return launch(col_pass<N, COL_Z_INV_FILTER>, ColSmem<N, COL_Z_INV_FILTER>::bytes, a, ColCfg<N>::T, s);
+      return launch<col_pass<N, COL_Z_INV_FILTER>>(ColSmem<N, COL_Z_INV_FILTER>::bytes, a, ColCfg<N>::T, s);
     case OP_COL_Z_INV:
-      return launch(col_pass<N, COL_Z_INV>, ColSmem<N, COL_Z_INV>::bytes, a, ColCfg<N>::T, s);
+      return launch<col_pass<N, COL_Z_INV>>(ColSmem<N, COL_Z_INV>::bytes, a, ColCfg<N>::T, s);
     case OP_COL_Y_INV:
-      return launch(col_pass<N, COL_Y_INV>, ColSmem<N, COL_Y_INV>::bytes, a, ColCfg<N>::T, s);
+      return launch<col_pass<N, COL_Y_INV>>(ColSmem<N, COL_Y_INV>::bytes, a, ColCfg<N>::T, s);
     case OP_COL_Z_FWD_PK:
-      return launch(col_pass<N, COL_Z_FWD_PK>, ColSmem<N, COL_Z_FWD_PK>::bytes, a, ColCfg<N>::T, s);
+      return launch<col_pass<N, COL_Z_FWD_PK>>(ColSmem<N, COL_Z_FWD_PK>::bytes, a, ColCfg<N>::T, s);
     case OP_ROW_R2C_SCALE:
-      return launch(row_r2c<N, PRO_SCALE>, RowSmem<N>::bytes, a, RowCfg<N>::T, s);
+      return launch<row_r2c<N, PRO_SCALE>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
     case OP_ROW_R2C_PK:
-      return launch(row_r2c<N, PRO_PK>, RowSmem<N>::bytes, a, RowCfg<N>::T, s);
+      return launch<row_r2c<N, PRO_PK>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
     case OP_ROW_C2R_STORE:
-      return launch(row_c2r<N, EPI_STORE>, RowSmem<N>::bytes, a, RowCfg<N>::T, s);
+      return launch<row_c2r<N, EPI_STORE>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
     case OP_ROW_C2R_IONIZE:
-      return launch(row_c2r<N, EPI_IONIZE>, RowSmem<N>::bytes, a, RowCfg<N>::T, s);
+      return launch<row_c2r<N, EPI_IONIZE>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
     default:
       return cudaErrorInvalidValue;
   }

@@ -30,7 +30,7 @@ def grf_z0(n: int, box_len: float, seed: int, cosmo: Cosmology = BASELINE_COSMO)
     nz = kmag > 0
     amp[nz] = np.sqrt(power_spectrum_z0(kmag[nz], cosmo) * n ** 3 / box_len ** 3)
     wk *= amp
-    return np.fft.irfftn(wk, s=(n, n, n))
+    return np.fft.irfftn(wk, s=(n, n, n), axes=(0, 1, 2))
 
 
 def density_box(n: int, box_len: float, seed: int, z: float, cosmo: Cosmology = BASELINE_COSMO,

@@ -133,13 +133,18 @@ def ionize_setup(n: int, box_len: float, z: float, *, zeta: float, t_vir_min: fl
                        update=int(update), ref_compat=bool(ref_compat))
 
 
+def delta_k(box_len: float) -> np.float32:
+    """DELTA_K = float32(2 pi / BOX_LEN) with BOX_LEN rounded to float32 (delta_T.py:51-52)."""
+    return np.float32(2.0 * math.pi / float(np.float32(box_len)))
+
+
 def pk_edges(n: int, box_len: float, num_bins: int, edge_dim: int | None = None) -> np.ndarray:
     """Bin edges K = logspace(log10 dk, log10(dk sqrt(3) DIM), NUM_BINS) as float32 (delta_T.py:87).
 
     The reference uses the large-box DIM for the top edge; by default the box's own HII_DIM is
     used (``edge_dim`` restores the reference's choice).
     """
-    dk = np.float32(2.0 * np.pi / np.float32(box_len))
+    dk = float(delta_k(box_len))
     top = edge_dim if edge_dim is not None else n
     return np.float32(np.logspace(np.log10(dk), np.log10(dk * np.sqrt(3.0) * top), num_bins))
 
@@ -151,7 +156,7 @@ def pk_k2_thresholds(n: int, box_len: float, edges: np.ndarray) -> np.ndarray:
     i.e. the first b with m <= T[b].  Deciding the comparison once, in float64 on the host,
     makes the bin of every mode identical on the GPU and in the oracle.
     """
-    dk = float(np.float32(2.0 * np.pi / np.float32(box_len)))
+    dk = float(delta_k(box_len))
     kmax2 = 3 * (n // 2) ** 2
     out = np.empty(len(edges), dtype=np.int64)
     for b, e in enumerate(np.asarray(edges, dtype=np.float64)):

@@ -45,6 +45,11 @@ def _fft(backend, workers):
             lambda a, **k: sf.irfftn(a, workers=workers, **k))
 
 
+def delta_k(box_len: float) -> float:
+    """float32(2 pi / float32(L)) as the reference's DELTA_K (delta_T.py:51-52)."""
+    return float(np.float32(2.0 * math.pi / float(np.float32(box_len))))
+
+
 def k2_grid(n: int) -> np.ndarray:
     """Integer |k / dk|^2 on the half-spectrum grid (n, n, n//2 + 1).
 
@@ -171,7 +176,7 @@ def conv_bubbles(deltax, setup, *, tol: float = 1e-5, backend: str = "numpy", wo
     d = (d * np.float32(setup.growth_scale)).astype(np.float64)    # cu: deltax *= fgrowth
     X = rfftn(d)
     k2 = k2_grid(n)
-    dk = float(np.float32(2.0 * np.pi / np.float32(setup.box_len)))
+    dk = delta_k(setup.box_len)
     dc = float(setup.deltac32)
     zeta = float(setup.zeta)
     flags = np.zeros((n, n, n), dtype=bool)
@@ -183,7 +188,7 @@ def conv_bubbles(deltax, setup, *, tol: float = 1e-5, backend: str = "numpy", wo
     steps = setup.steps if max_radii is None else setup.steps[:max_radii]
     for st in steps:
         W = window(k2, dk, float(st.R), setup.filter_type, setup.ref_compat) / float(n) ** 3
-        dR = irfftn(X * W, s=(n, n, n)) * float(n) ** 3
+        dR = irfftn(X * W, s=(n, n, n), axes=(0, 1, 2)) * float(n) ** 3
         f = erfc((dc - dR) / float(st.denom))
         m = float(np.mean(f))
         means.append(m)
@@ -210,7 +215,8 @@ def conv_bubbles(deltax, setup, *, tol: float = 1e-5, backend: str = "numpy", wo
         exempt = maybe & ~sure
     if ionized is None:      # bounded sample ended before the final radius
         ionized = flags.astype(np.float64)
-    return {"ionized": ionized, "flags": flags, "exempt": exempt, "means": np.array(means)}
+    return {"ionized": ionized, "flags": flags, "exempt": exempt, "means": np.array(means),
+            "max_margin": max_margin if setup.update == 0 else None}
 
 
 def delta_T(xH, deltax, const_factor: float):
@@ -235,7 +241,7 @@ def power_spectrum(dT, ave: float, box_len: float, edges, *, dimensional: bool =
         g = g * ave
     G = rfftn(g)
     k2 = k2_grid(n)
-    dk = float(np.float32(2.0 * np.pi / np.float32(box_len)))
+    dk = delta_k(box_len)
     kmag = dk * np.sqrt(k2.astype(np.float64))
     wgt = np.full(k2.shape, 2.0)
     wgt[:, :, 0] = 1.0

@@ -44,16 +44,20 @@ def _setup(n, L, z, **kw):
 
 
 def _compare_ionized(ion_gpu, ref, label=""):
+    """Every cell outside the oracle's exemption band must match the oracle's ionised fraction.
+
+    Loop radii decide flags (a flip there changes the cell from 1 to a partial value, far
+    beyond the tolerance); the final radius is continuous at the threshold (zeta f -> 1 from
+    below meets the flagged value 1), so it needs no exemption.
+    """
     ion_o = ref["ionized"]
     ex = ref["exempt"]
-    flags_g = ion_gpu >= 1.0
-    flags_o = ion_o >= 1.0
-    bad = (flags_g != flags_o) & ~ex
-    assert bad.sum() == 0, f"{label}: {int(bad.sum())} non-exempt flag mismatches (exempt {int(ex.sum())})"
-    both = ~ex & ~flags_o
-    if both.any():
-        err = np.abs(ion_gpu[both] - ion_o[both]).max()
-        assert err <= PARTIAL_ATOL, f"{label}: partial ionisation differs by {err}"
+    diff = np.abs(ion_gpu - ion_o)
+    bad = (diff > PARTIAL_ATOL) & ~ex
+    assert bad.sum() == 0, (f"{label}: {int(bad.sum())} cells differ by more than {PARTIAL_ATOL} outside "
+                            f"the {int(ex.sum())} exempt cells (max {diff[~ex].max():.3g})")
+    loop_flags = ref["flags"]
+    assert np.all(ion_gpu[loop_flags & ~ex] == 1.0), f"{label}: oracle-flagged cells not ionised"
     xg, xo = 1.0 - ion_gpu.mean(), 1.0 - ion_o.mean()
     assert abs(xg - xo) <= MEAN_RTOL * abs(xo) + 1e-7, f"{label}: mean x_HI {xg} vs {xo}"
 

@@ -1,0 +1,249 @@
+"""CPU tests: the oracle and the host layer against the reference's tables and hand-derived cases."""
+import math
+import os
+
+import numpy as np
+import pytest
+from scipy.special import erfc
+
+from conftest import module
+from oracle import es_oracle as O
+
+cos = module("cosmology")
+sch = module("schedule")
+grf = module("grf")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+# ---------------------------------------------------------------- sigma^2(R): the reference's KAT
+def test_sigma2_integrator_reproduces_reference_sig0_table():
+    g = np.load(os.path.join(GOLDEN, "sigma_kat.npz"))
+    table = cos.SigmaTable((g["k"], g["Del2"]))
+    rel = np.array([table.sigma2(R) / s - 1.0 for R, s in zip(g["radius"], g["sig0"])])
+    # sig0.npz was integrated with scipy quad, the reference's sig0() uses a 1000-point trapezoid
+    assert np.abs(rel).max() < 2e-4, np.abs(rel).max()
+
+
+def test_sigma8_normalisation_and_transfer_function_against_reference_table():
+    g = np.load(os.path.join(GOLDEN, "sigma_kat.npz"))
+    planck = cos.PLANCK13
+    t = cos.SigmaTable(planck)
+    assert abs(math.sqrt(t.sigma2(8.0 / planck.h)) - planck.sigma_8) < 2e-4
+    # the reference's Delta^2(k) came from cosmolopy's Eisenstein & Hu fit (with baryon
+    # wiggles); the zero-wiggle form here stays within 2% of it across 1e-4 < k < 100 /Mpc
+    k = g["k"]
+    m = (k > 1e-4) & (k < 100)
+    r = cos.del2_z0(k[m], planck) / g["Del2"][m]
+    assert np.abs(r - 1).max() < 0.02
+    assert abs(np.median(r) - 1) < 1e-3
+
+
+def test_growth_and_barrier():
+    c = cos.BASELINE_COSMO
+    assert cos.growth_factor(0.0, c) == pytest.approx(1.0)
+    # matter domination: D ~ a at high z, within the Lambda correction
+    d10, d20 = cos.growth_factor(10.0, c), cos.growth_factor(20.0, c)
+    assert d10 / d20 == pytest.approx(21.0 / 11.0, rel=2e-3)
+    s, dc = cos.sig_del(1e4, 8.0, c)
+    assert dc == pytest.approx(1.686 / cos.growth_factor(8.0, c))
+    # T_vir = 1e4 K at z = 8 is a ~1e8 Msun halo (mu = 0.59), sigma(M) ~ 5.5 at z = 0
+    assert 3e7 < cos.virial_mass(1e4, 8.0, c) < 3e8
+    assert 4.5 < s < 6.5
+    assert cos.collapse_fraction(s, dc) == pytest.approx(math.erfc(dc / (math.sqrt(2) * s)))
+
+
+# ---------------------------------------------------------------- radius schedule
+@pytest.mark.parametrize("spec,count", [(grf.single_64(), 29), (grf.sweep_256()[0], 32), (grf.single_512(), 40)])
+def test_radius_schedule_lengths(spec, count):
+    st = sch.ionize_setup(spec.n, spec.box_len, spec.z, zeta=spec.zeta, t_vir_min=spec.t_vir_min,
+                          R_max=spec.R_max, cosmo=cos.BASELINE_COSMO)
+    assert st.n_radii == count
+    R = st.radii()
+    assert R[0] == np.float32(spec.R_max)
+    assert np.all(np.diff(R) < 0)
+    assert np.allclose(R[:-1] / R[1:], 1.1, rtol=1e-6)
+    assert [s.final for s in st.steps] == [False] * (count - 1) + [True]
+    # stop rule of find_HII_bubbles.py:123
+    cell = sch.L_FACTOR * spec.box_len / spec.n
+    assert float(R[-1]) / 1.1 <= cell and float(R[-2]) / 1.1 > cell
+    assert np.all(st.denoms() > 0)
+
+
+def test_schedule_raises_like_reference():
+    # sigma^2 at the cell scale above sigma_min^2 -> the reference raises (l.116-118)
+    with pytest.raises(sch.ExcursionSetError):
+        sch.ionize_setup(64, 10.0, 8.0, zeta=30.0, t_vir_min=1e5, R_max=15.0, R_min=0.01,
+                         cosmo=cos.BASELINE_COSMO)
+    with pytest.raises(sch.ExcursionSetError):
+        sch.ionize_setup(63, 100.0, 8.0, zeta=30.0, t_vir_min=1e4, R_max=15.0, cosmo=cos.BASELINE_COSMO)
+    with pytest.raises(sch.ExcursionSetError):
+        sch.ionize_setup(64, 100.0, 8.0, zeta=-1.0, t_vir_min=1e4, R_max=15.0, cosmo=cos.BASELINE_COSMO)
+
+
+def test_single_radius_schedule():
+    st = sch.ionize_setup(32, 48.0, 8.0, zeta=30.0, t_vir_min=1e4, R_max=1.0, cosmo=cos.BASELINE_COSMO)
+    assert st.n_radii == 1 and st.steps[0].final
+
+
+# ---------------------------------------------------------------- filter windows
+def test_window_closed_forms_and_fallthrough():
+    dk, R = 0.1, 3.0
+    k2 = np.array([0, 1, 4, 9, 50, 200, 1000])
+    kR = dk * np.sqrt(k2) * R
+    w0 = O.window(k2, dk, R, 0, False)
+    ref0 = np.where(kR > 0, 3 * (np.sin(kR) - kR * np.cos(kR)) / np.where(kR > 0, kR, 1) ** 3, 1.0)
+    assert np.allclose(w0, ref0, rtol=1e-9, atol=1e-12)
+    w1 = O.window(k2, dk, R, 1, False)
+    assert np.array_equal(w1, (kR * 0.413566994 <= 1).astype(float))
+    w2 = O.window(k2, dk, R, 2, False)
+    assert np.allclose(w2, np.exp(-(0.643 * kR) ** 2 / 2))
+    # reference switch fall-through: case 0 -> 1 -> 2
+    wc0 = O.window(k2, dk, R, 0, True)
+    x = kR * 0.413566994
+    want = ref0 * (x <= 1) * np.exp(-(0.643 * x) ** 2 / 2)
+    assert np.allclose(wc0, want, rtol=1e-9, atol=1e-15)
+    wc1 = O.window(k2, dk, R, 1, True)
+    assert np.allclose(wc1, (x <= 1) * np.exp(-(0.643 * x) ** 2 / 2))
+    assert np.allclose(O.window(k2, dk, R, 2, True), w2)
+
+
+def test_series_window_continuity():
+    x = np.array([1e-6, 1e-3, 9.99e-3, 1.001e-2, 0.5])
+    direct = 3 * (np.sin(x) - x * np.cos(x)) / x ** 3
+    assert np.allclose(O.rtophat(x)[2:], direct[2:], rtol=1e-7)
+    assert abs(O.rtophat(np.array([1e-6]))[0] - 1.0) < 1e-12
+
+
+def test_single_mode_is_filtered_exactly():
+    # delta = A cos(2 pi m x / L): delta_R = A W(k_m R) cos(...) for every filter
+    n, L, m = 16, 32.0, 3
+    x = np.arange(n)
+    d = (0.5 * np.cos(2 * np.pi * m * x / n))[None, None, :] * np.ones((n, n, 1))
+    dk = O.delta_k(L)
+    X = np.fft.rfftn(d)
+    for fil in (0, 1, 2):
+        W = O.window(O.k2_grid(n), dk, 2.0, fil, False)
+        out = np.fft.irfftn(X * W, s=(n, n, n), axes=(0, 1, 2))
+        assert np.allclose(out, d * O.window(np.array([m * m]), dk, 2.0, fil, False)[0], atol=1e-12)
+
+
+# ---------------------------------------------------------------- ionisation cases
+def _setup(n=32, L=48.0, z=8.0, **kw):
+    args = dict(zeta=30.0, t_vir_min=1e4, R_max=15.0, cosmo=cos.BASELINE_COSMO)
+    args.update(kw)
+    return sch.ionize_setup(n, L, z, **args)
+
+
+def test_uniform_density_hand_derived():
+    for zeta in (40.0, 20.0):
+        st = _setup(zeta=zeta)
+        r = O.conv_bubbles(np.full((32, 32, 32), 0.3, np.float32), st)
+        fc = float(st.fc_mean_ps)
+        want = 1.0 if zeta * fc >= 1 else zeta * fc
+        assert np.allclose(r["ionized"], want, atol=1e-12)
+
+
+def test_linear_mode_skips_normalisation():
+    st = _setup(linear=True)
+    assert not st.normalize_mean and st.growth_scale == 1.0
+    d = np.zeros((32, 32, 32), np.float32)
+    r = O.conv_bubbles(d, st)
+    # delta = 0 everywhere: f = erfc(delta_c / denom_final), no rescale
+    f = erfc(float(st.deltac32) / float(st.steps[-1].denom))
+    want = 1.0 if st.zeta * f >= 1 else st.zeta * f
+    assert np.allclose(r["ionized"], want, atol=1e-12)
+
+
+def test_oracle_matches_committed_fixture():
+    g = np.load(os.path.join(GOLDEN, "oracle_32.npz"))
+    d = grf.density_box(32, 48.0, seed=0, z=8.0)
+    assert np.array_equal(d, g["density"]), "seeded density changed"
+    for name, kw in [("center", {}), ("sphere", {"update": 1, "R_max": 10.0})]:
+        st = _setup(**kw)
+        assert np.array_equal(st.radii(), g[f"{name}_radii"])
+        assert np.array_equal(st.denoms(), g[f"{name}_denoms"])
+        r = O.conv_bubbles(d, st)
+        ex = np.unpackbits(g[f"{name}_exempt"])[: d.size].reshape(d.shape).astype(bool)
+        assert np.array_equal(r["exempt"], ex)
+        assert np.allclose(r["ionized"], g[f"{name}_ionized"], atol=1e-9)
+
+
+def test_sphere_painting_against_brute_force():
+    rng = np.random.default_rng(3)
+    n = 10
+    c = rng.random((n, n, n)) < 0.01
+    for r2max, periodic in [(0, True), (2, True), (5, False), (9, True), (13, False)]:
+        got = O.paint_spheres(c, r2max, periodic)
+        want = np.zeros_like(c)
+        idx = np.indices((n, n, n)).reshape(3, -1).T
+        for cz, cy, cx in np.argwhere(c):
+            d = idx - np.array([cz, cy, cx])
+            if periodic:
+                d = (d + n // 2) % n - n // 2
+                # nearest image distance along each axis
+                d = np.minimum(np.abs(d), n - np.abs(d))
+            want.reshape(-1)[(d ** 2).sum(1) <= r2max] = True
+        assert np.array_equal(got, want), (r2max, periodic)
+
+
+def test_sphere_radius_rules():
+    assert O.sphere_r2max(2.0, 1.0, False) == 3          # |d|^2 < 4
+    assert O.sphere_r2max(2.0001, 1.0, False) == 4
+    assert O.sphere_r2max(3.0, 1.5, False) == 3          # R in cells = 2
+    assert O.sphere_r2max(3.0, 1.5, True) == 8           # reference: R in Mpc as cells
+
+
+# ---------------------------------------------------------------- delta_T and P(k)
+def test_power_spectrum_half_spectrum_weights_match_full_fft():
+    rng = np.random.default_rng(1)
+    n, L = 12, 30.0
+    dT = 10 + rng.standard_normal((n, n, n))
+    ave = dT.mean()
+    edges = sch.pk_edges(n, L, 6)
+    _, k_ave, ps_ave, cnt = O.power_spectrum(dT, ave, L, edges)
+    # brute force over the full complex spectrum (what pbox_kernel loops over)
+    g = (dT / ave - 1) * L ** 3 / n ** 3
+    G = np.fft.fftn(g)
+    dk = O.delta_k(L)
+    ps = np.zeros(6); ks = np.zeros(6); ct = np.zeros(6)
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                w = [v - n if v > n // 2 else v for v in (k, j, i)]
+                m2 = sum(v * v for v in w)
+                if m2 == 0:
+                    continue
+                km = dk * math.sqrt(m2)
+                b = int(np.searchsorted(edges.astype(np.float64), km, side="left"))
+                if b >= 6:
+                    continue
+                ps[b] += km ** 3 * abs(G[k, j, i]) ** 2 / (2 * np.pi ** 2 * L ** 3)
+                ks[b] += km
+                ct[b] += 1
+    assert np.array_equal(cnt, ct)
+    nz = ct > 0
+    assert np.allclose(ps_ave[nz], ps[nz] / ct[nz], rtol=1e-10)
+    assert np.allclose(k_ave[nz], ks[nz] / ct[nz], rtol=1e-12)
+
+
+def test_pk_thresholds_follow_first_edge_rule():
+    n, L = 64, 100.0
+    edges = sch.pk_edges(n, L, 20)
+    thr = sch.pk_k2_thresholds(n, L, edges)
+    dk = O.delta_k(L)
+    for m in range(0, 3 * 32 ** 2 + 1, 7):
+        by_thr = next((b for b, t in enumerate(thr) if m <= t), len(thr))
+        by_edge = int(np.searchsorted(edges.astype(np.float64), dk * math.sqrt(m), side="left"))
+        assert by_thr == by_edge, m
+    assert edges.dtype == np.float32 and edges[0] == np.float32(dk)
+
+
+def test_delta_T_factor_matches_reference_formula():
+    c = cos.PLANCK13
+    z = 9.0
+    want = 27 * (c.omega_b_0 * c.h ** 2 / 0.023) * np.sqrt((0.15 / c.omega_M_0 / c.h ** 2) * (1 + z) / 10.0)
+    assert cos.brightness_temperature_factor(z, c) == pytest.approx(want, rel=1e-14)
+    g = np.load(os.path.join(GOLDEN, "oracle_32.npz"))
+    dT, ave = O.delta_T((1 - g["center_ionized"]).astype(np.float32), g["density"],
+                        cos.brightness_temperature_factor(8.0, cos.BASELINE_COSMO))
+    assert np.allclose(dT, g["dT"], rtol=1e-12) and ave == pytest.approx(float(g["ave"]), rel=1e-12)
