@@ -13,6 +13,10 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libes_engine.so"
 
 ES_OK = 0
+# kernel kinds reported by es_profile_read (ES_PROF_* in include/es_engine.h)
+PROF_KINDS = ("col_z_fwd", "col_y_fwd", "col_z_inv_filter", "col_y_inv", "col_z_fwd_pk", "row_r2c",
+              "row_r2c_pk", "row_c2r", "row_c2r_ionize", "col_z_inv", "filter_table", "final",
+              "delta_T", "paint")
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "unsupported box size"}
 
 
@@ -53,6 +57,9 @@ _PROTOS = {
                                     C.c_void_p, C.c_void_p]),
     "es_fft_r2c": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "es_fft_c2r": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "es_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
+    "es_profile_reset": (C.c_int, [C.c_void_p]),
+    "es_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_int]),
     "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_version": (C.c_int, []),
 }

@@ -94,6 +94,11 @@ struct es_plan {
   int* h_thr = nullptr;
   cudaEvent_t staged = nullptr;     // last upload from the staging buffers
   size_t partial_floats = 0;
+  // optional per-launch timing: event pairs around every kernel while enabled
+  std::vector<cudaEvent_t> prof_events;
+  std::vector<int> prof_ops;
+  int prof_used = 0;
+  int prof_dropped = 0;
 };
 
 namespace {
@@ -317,9 +322,24 @@ es::OpArgs base_args(const es_plan* p) {
   return a;
 }
 
-int run_op(const es_plan* p, int op, es::OpArgs a, int grid, cudaStream_t s) {
+// Records the start event of a timed launch; returns the slot or -1 when timing is off/full.
+int prof_begin(es_plan* p, int op, cudaStream_t s) {
+  if (p->prof_events.empty()) return -1;
+  if (2 * (p->prof_used + 1) > (int)p->prof_events.size()) { ++p->prof_dropped; return -1; }
+  const int slot = p->prof_used++;
+  p->prof_ops[slot] = op;
+  cudaEventRecord(p->prof_events[2 * slot], s);
+  return slot;
+}
+void prof_end(es_plan* p, int slot, cudaStream_t s) {
+  if (slot >= 0) cudaEventRecord(p->prof_events[2 * slot + 1], s);
+}
+
+int run_op(es_plan* p, int op, es::OpArgs a, int grid, cudaStream_t s) {
   a.grid = grid;
+  const int slot = prof_begin(p, op, s);
   cudaError_t e = p->size->launch(op, &a, s);
+  prof_end(p, slot, s);
   if (e != cudaSuccess) return fail(ES_E_CUDA, "kernel op %d (n=%d) launch failed: %s", op, p->n, cudaGetErrorString(e));
   return ES_OK;
 }
@@ -450,6 +470,7 @@ int es_plan_destroy(es_plan* p) {
   if (p->h_rad) cudaFreeHost(p->h_rad);
   if (p->h_thr) cudaFreeHost(p->h_thr);
   if (p->staged) cudaEventDestroy(p->staged);
+  for (cudaEvent_t e : p->prof_events) cudaEventDestroy(e);
   delete p;
   return ES_OK;
 }
@@ -505,8 +526,10 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
   ES_CUDA(cudaMemcpyAsync(p->rad, p->h_rad, sizeof(RadDev) * nr, cudaMemcpyHostToDevice, s));
   ES_CUDA(cudaEventRecord(p->staged, s));
   const float inv_n3 = (float)(1.0 / ((double)p->n * p->n * p->n));
+  int slot = prof_begin(p, ES_PROF_FILTER_TABLE, s);
   filter_table_kernel<<<p->sms * 4, 256, 0, s>>>(p->wtab, p->k2n, p->rad, nr, p->dk, prm->filter_type,
                                                    prm->ref_compat, inv_n3);
+  prof_end(p, slot, s);
   ES_CUDA(cudaGetLastError());
   const size_t N3 = (size_t)p->n * p->n * p->n;
   ES_CUDA(cudaMemsetAsync(p->flags, 0, N3 / 8, s));
@@ -540,15 +563,19 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     a.normalize = prm->normalize_mean;
     if ((rc = run_op(p, es::OP_ROW_C2R_IONIZE, a, grid_row(p), s))) return rc;
     if (prm->update == 1 && r > 0) {
+      slot = prof_begin(p, ES_PROF_PAINT, s);
       paint_kernel<<<p->sms * 4, 256, 0, s>>>(p->centers, p->counters + 1, p->flags, p->n,
                                               p->h_rad[r - 1].r2max, prm->ref_compat ? 0 : 1);
+      prof_end(p, slot, s);
       ES_CUDA(cudaGetLastError());
     }
   }
+  slot = prof_begin(p, ES_PROF_FINAL, s);
   final_kernel<256><<<grid_elem(p), 256, 0, s>>>(
       reinterpret_cast<const float2*>(p->dR[(nr - 1) & 1]), p->flags, (long)(N3 / 2), prm->delta_c,
       prm->radii[nr - 1].denom, p->stats + (size_t)(nr - 1) * kStatsStride, prm->zeta, inv_zeta,
       prm->output, reinterpret_cast<float2*>(out), p->partials, p->counters, nf, inv_n3);
+  prof_end(p, slot, s);
   ES_CUDA(cudaGetLastError());
   return ES_OK;
 }
@@ -557,9 +584,11 @@ int es_delta_T(es_plan* p, const float* xH, const float* delta, float c, float* 
   if (!p || !xH || !delta || !dT || !ave) return fail(ES_E_ARG, "es_delta_T: NULL argument");
   DeviceGuard g(p->device);
   const size_t N3 = (size_t)p->n * p->n * p->n;
+  const int slot = prof_begin(p, ES_PROF_DELTA_T, (cudaStream_t)stream);
   delta_T_kernel<256><<<grid_elem(p), 256, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(xH), reinterpret_cast<const float2*>(delta), (long)(N3 / 2), c,
       reinterpret_cast<float2*>(dT), p->partials, p->counters, ave, (float)(1.0 / (double)N3));
+  prof_end(p, slot, (cudaStream_t)stream);
   ES_CUDA(cudaGetLastError());
   return ES_OK;
 }
@@ -623,6 +652,44 @@ int es_fft_c2r(es_plan* p, const void* in, float* out, void* stream) {
   a.cin = p->T;
   a.rout = reinterpret_cast<float2*>(out);
   return run_op(p, es::OP_ROW_C2R_STORE, a, grid_row(p), s);
+}
+
+int es_profile_enable(es_plan* p, int max_launches) {
+  if (!p || max_launches < 0 || max_launches > (1 << 22)) return fail(ES_E_ARG, "es_profile_enable: bad arguments");
+  DeviceGuard g(p->device);
+  ES_CUDA(cudaDeviceSynchronize());
+  for (cudaEvent_t e : p->prof_events) cudaEventDestroy(e);
+  p->prof_events.clear();
+  p->prof_ops.assign(max_launches, -1);
+  p->prof_used = 0;
+  p->prof_dropped = 0;
+  for (int i = 0; i < 2 * max_launches; ++i) {
+    cudaEvent_t e;
+    ES_CUDA(cudaEventCreate(&e));
+    p->prof_events.push_back(e);
+  }
+  return ES_OK;
+}
+
+int es_profile_reset(es_plan* p) {
+  if (!p) return fail(ES_E_ARG, "es_profile_reset: NULL plan");
+  p->prof_used = 0;
+  p->prof_dropped = 0;
+  return ES_OK;
+}
+
+int es_profile_read(es_plan* p, float* total_ms, int* counts, int nops) {
+  if (!p || !total_ms || !counts || nops < ES_PROF_COUNT) return fail(ES_E_ARG, "es_profile_read: bad arguments");
+  DeviceGuard g(p->device);
+  for (int i = 0; i < nops; ++i) { total_ms[i] = 0.f; counts[i] = 0; }
+  for (int k = 0; k < p->prof_used; ++k) {
+    float ms = 0.f;
+    ES_CUDA(cudaEventSynchronize(p->prof_events[2 * k + 1]));
+    ES_CUDA(cudaEventElapsedTime(&ms, p->prof_events[2 * k], p->prof_events[2 * k + 1]));
+    const int op = p->prof_ops[k];
+    if (op >= 0 && op < nops) { total_ms[op] += ms; counts[op] += 1; }
+  }
+  return p->prof_dropped;
 }
 
 }  // extern "C"

@@ -166,6 +166,24 @@ class ExcursionSetPlan:
         _lib.check("es_fft_c2r", self.lib.es_fft_c2r(self.handle, _ptr(X), _ptr(out), _stream_handle(self.device, stream)), self.lib)
         return out
 
+    # ------------------------------------------------------------------ per-launch timing
+    def profile_enable(self, max_launches: int):
+        """Bracket each kernel this plan launches with CUDA events (0 turns it off)."""
+        _lib.check("es_profile_enable", self.lib.es_profile_enable(self.handle, int(max_launches)), self.lib)
+
+    def profile_reset(self):
+        _lib.check("es_profile_reset", self.lib.es_profile_reset(self.handle), self.lib)
+
+    def profile_read(self) -> dict:
+        """{kernel kind: (total ms, launches)} for the launches since the last reset."""
+        k = len(_lib.PROF_KINDS)
+        ms = (C.c_float * k)()
+        cnt = (C.c_int * k)()
+        rc = self.lib.es_profile_read(self.handle, ms, cnt, k)
+        if rc < 0:
+            _lib.check("es_profile_read", rc, self.lib)
+        return {name: (float(ms[i]), int(cnt[i])) for i, name in enumerate(_lib.PROF_KINDS) if cnt[i]}
+
     def close(self):
         if getattr(self, "_h", None) is not None:
             self.lib.es_plan_destroy(self._h)

@@ -1,0 +1,388 @@
+#!/usr/bin/env python
+"""Excursion-set benchmark: voxel-radius updates/s of the HII_DIM=256 sweep on GB300.
+
+Workload (one step): 52 density boxes of 256^3 cells, BOX_LEN = 300 Mpc (seeds 0-3 x z = 6.0,
+6.5, ..., 12.0, Gaussian random fields with the BBKS spectrum), each run through the whole path:
+forward transform, 32 radii of the excursion-set loop (zeta = 30, R_mfp = 15 Mpc,
+Tvir = 1e4 K, real-space top-hat), final partial ionisation, delta_T and a 20-bin P(k).
+
+Printed JSON line (rank 0): ``value`` = voxel-radius updates / s with inputs resident in HBM,
+``e2e`` = the same metric through ``Programs.pipeline.simulate_box`` with pinned host buffers
+(host<->device copies inside the timed region), ``roofline`` for the dominant kernel from
+per-launch CUDA events over the timed region, ``cpu_baseline`` = the FP64 numpy oracle on a
+bounded sample of the same workload on the host cores.
+
+``--impl reference`` times the oracle port of the reference path (there is no runnable
+reference implementation: Python 2 + PyCUDA + pyfft + cosmolopy) on all host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel-radius updates/s @256^3 (fused excursion-set engine)"
+UNIT = "voxel-radius updates/s"
+N = 256
+BOX_LEN = 300.0
+NUM_BINS = 20
+
+# Algorithmic bytes per voxel for one launch of each kernel kind: what the kernel must read and
+# write at minimum (half spectrum = 8 B x (N/2+1)/N per real voxel, ~4.03 B at 256^3).
+HALF = 8.0 * (N // 2 + 1) / N
+
+
+def kernel_bytes_per_voxel() -> dict:
+    return {
+        "col_z_inv_filter": 2 * HALF,                 # read spectrum, write filtered intermediate
+        "col_y_inv": 2 * HALF,                        # read + write intermediate
+        "row_c2r_ionize": HALF + 4 + 4 + 2 * 0.125,   # read spectrum, write delta_R, read previous delta_R, flag bits r+w
+        "row_r2c": 4 + HALF,
+        "col_y_fwd": 2 * HALF,
+        "col_z_fwd": 2 * HALF,
+        "final": 4 + 0.125 + 4,
+        "delta_T": 12.0,
+        "row_r2c_pk": 4 + HALF,
+        "col_z_fwd_pk": HALF,
+        "filter_table": 0.0,
+    }
+
+
+# whole-path algorithmic bytes: 22 B per voxel-radius, 20 B per voxel-box (forward transform +
+# x_HI write), 24 B per voxel for delta_T and P(k)
+B_RADIUS, B_BOX, B_DT_PK = 22.0, 20.0, 24.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "", 1).isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i - 5] for r in self.rows for i in range(5, 9) if r[i].lower() == "active"})
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_workload(rank: int, boxes: int):
+    grf = importlib.import_module("21cmpy_gb300.grf")
+    specs = grf.sweep_256()[:boxes]
+    # weak scaling: rank r takes seeds 4r..4r+3 of the same redshift grid
+    base = {}
+    out = []
+    for s in specs:
+        seed = s.seed + 4 * rank
+        if seed not in base:
+            base[seed] = grf.grf_z0(s.n, s.box_len, seed)
+        out.append((s, seed, grf.density_box(s.n, s.box_len, seed, s.z, base=base[seed])))
+    return out
+
+
+def setups_for(work):
+    cos = importlib.import_module("21cmpy_gb300.cosmology")
+    sch = importlib.import_module("21cmpy_gb300.schedule")
+    res = []
+    for s, _seed, _d in work:
+        st = sch.ionize_setup(s.n, s.box_len, s.z, zeta=s.zeta, t_vir_min=s.t_vir_min, R_max=s.R_max,
+                              cosmo=cos.BASELINE_COSMO)
+        res.append((st, cos.brightness_temperature_factor(s.z, cos.BASELINE_COSMO)))
+    return res
+
+
+def cpu_baseline(work, setups, radii: int) -> dict:
+    """FP64 numpy oracle (numpy.fft, one thread) on the first `radii` radii of one box."""
+    from oracle import es_oracle as O
+    s, _seed, d = work[0]
+    st, _c = setups[0]
+    t0 = time.perf_counter()
+    O.conv_bubbles(d, st, max_radii=radii)
+    dt = time.perf_counter() - t0
+    return {"value": N ** 3 * radii / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"one 256^3 box (seed {_seed}, z={s.z}), forward FFT + first {radii} of {st.n_radii} radii, "
+                      f"numpy.fft float64 single thread, {dt:.1f} s"}
+
+
+def run_reference(args):
+    """Reference arm: the oracle port of the path on all host cores (scipy.fft workers)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import es_oracle as O
+    work = make_workload(0, 1)
+    setups = setups_for(work)
+    s, _seed, d = work[0]
+    st, _c = setups[0]
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    radii = args.ref_radii
+
+    def step():
+        O.conv_bubbles(d, st, backend="scipy", workers=cores, max_radii=radii)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = N ** 3 * radii * args.steps / dt
+    sample = (f"one 256^3 box per step (seed 0, z={s.z}), forward FFT + first {radii} of {st.n_radii} radii, "
+              f"float64 scipy.fft with {cores} workers")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded BBKS Gaussian random fields)",
+            "config": {"workload": "excursion-set sweep 256^3 (bounded CPU sample)", "n": N, "box_len_mpc": BOX_LEN},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--boxes", type=int, default=52, help="boxes per step (the sweep has 52)")
+    ap.add_argument("--cpu-radii", type=int, default=6, help="radii in the timed CPU sample")
+    ap.add_argument("--ref-radii", type=int, default=4, help="radii per reference-arm step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps")
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else torch.cuda.current_device())
+    torch.cuda.set_device(dev)
+
+    import __graft_entry__
+    __graft_entry__.build()
+    eng = importlib.import_module("21cmpy_gb300.engine")
+    sch = importlib.import_module("21cmpy_gb300.schedule")
+
+    work = make_workload(rank, args.boxes)
+    setups = setups_for(work)
+    edges = sch.pk_edges(N, BOX_LEN, NUM_BINS)
+    nboxes = len(work)
+    dens = [torch.from_numpy(d).to(dev) for _s, _seed, d in work]
+    xh = [torch.empty((N, N, N), dtype=torch.float32, device=dev) for _ in range(nboxes)]
+    dT = [torch.empty((N, N, N), dtype=torch.float32, device=dev) for _ in range(nboxes)]
+    nf = torch.empty((nboxes, 1), dtype=torch.float32, device=dev)
+    ave = torch.empty((nboxes, 1), dtype=torch.float32, device=dev)
+    pk = torch.empty((nboxes, 3, NUM_BINS), dtype=torch.float32, device=dev)
+    plan = eng.ExcursionSetPlan(N, BOX_LEN, max_radii=64, device=dev)
+    updates_per_step = sum(N ** 3 * st.n_radii for st, _c in setups)
+
+    def step():
+        for i in range(nboxes):
+            st, c = setups[i]
+            plan.run(dens[i], st, out=xh[i], nf=nf[i])
+            plan.delta_T(xh[i], dens[i], c, out=dT[i], ave=ave[i])
+            plan.power_spectrum(dT[i], ave[i], edges, out=pk[i])
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    # launches per step, to size the event pool of the timed region
+    launches_per_box = 3 + 1 + 3 * max(st.n_radii for st, _c in setups) + 1 + 1 + 3
+    plan.profile_enable(launches_per_box * nboxes * args.steps + 16)
+    stream = torch.cuda.current_stream(dev)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    barrier()
+    clock_info = clocks.stop()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    prof = plan.profile_read()
+    plan.profile_enable(0)
+    if dist is not None:
+        t = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = updates_per_step * world * args.steps / elapsed
+
+    # dominant kernel roofline from the per-launch events of the timed region
+    hbm, peak_kind = peaks()
+    bpv = kernel_bytes_per_voxel()
+    dom = max((k for k in prof if k in bpv), key=lambda k: prof[k][0])
+    dom_ms, dom_count = prof[dom]
+    dom_bytes = bpv[dom] * N ** 3
+    achieved = dom_bytes * dom_count / (dom_ms / 1e3) / 1e9
+    traffic = measured_traffic(dom)
+    radii_total = sum(st.n_radii for st, _c in setups)
+    path_bytes = (B_RADIUS * N ** 3 * radii_total + (B_BOX + B_DT_PK) * N ** 3 * nboxes) * args.steps * world
+    path_gbs = path_bytes / elapsed / 1e9
+
+    # end-to-end through the public host-buffer API (pinned host inputs/outputs)
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, work, dev, barrier, dist)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded BBKS Gaussian random fields, Om=0.31 Ob=0.049 h=0.68 s8=0.81)",
+        "config": {"workload": f"excursion-set sweep: {nboxes} boxes of 256^3 per GPU (seeds 0-3 x z=6.0..12.0 step 0.5), "
+                               "BOX_LEN=300 Mpc, zeta=30, R_mfp=15 Mpc, Tvir=1e4 K, real-space top-hat, "
+                               f"{radii_total // nboxes} radii/box, delta_T + {NUM_BINS}-bin P(k)",
+                   "n": N, "box_len_mpc": BOX_LEN, "boxes_per_gpu": nboxes, "radii_per_box": radii_total // nboxes,
+                   "l2": "no flush: every box's inputs (64 MiB density + 64 MiB spectrum) and its 256 MiB working "
+                         "set exceed the 129 MB L2, and consecutive boxes touch different inputs",
+                   "parallelism": f"{world} independent GPU(s), boxes sharded by seed, no collective"},
+        "gpu_launches": int(sum(c for _ms, c in prof.values())),
+        "kernel_ms": {k: round(v[0], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_ms / dom_count,
+                     "traffic": traffic},
+        "path_roofline": {"achieved": path_gbs, "peak": hbm, "unit": "GB/s", "frac": path_gbs / hbm,
+                          "bytes_model": "22 B/voxel-radius + 20 B/voxel-box + 24 B/voxel delta_T+P(k)"},
+        "clocks": clock_info,
+    }
+    if e2e is not None:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(work, setups, args.cpu_radii)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(args, work, dev, barrier, dist):
+    import torch
+    pipe = importlib.import_module("21cmpy_gb300.Programs.pipeline")
+    cos = importlib.import_module("21cmpy_gb300.cosmology")
+    params = {"ZETA": 30.0, "ION_Tvir_MIN": 1e4, "R_BUBBLE_MAX": 15.0, "R_BUBBLE_MIN": 0.5, "DELTA_R_FACTOR": 1.1,
+              "COSMO": cos.BASELINE_COSMO, "NUM_BINS": NUM_BINS, "DIMENSIONAL_T_POWER_SPEC": False}
+    host_in = [torch.from_numpy(d).pin_memory() for _s, _seed, d in work]
+    xh_out = [torch.empty((N, N, N), dtype=torch.float32).pin_memory() for _ in work]
+    dT_out = [torch.empty((N, N, N), dtype=torch.float32).pin_memory() for _ in work]
+    pd = {"BoxSize": BOX_LEN, "HIIdim": N}
+
+    def step():
+        radii = 0
+        for i, (s, _seed, _d) in enumerate(work):
+            r = pipe.simulate_box(host_in[i], pd, Z=s.z, fil=0, params=params, xH_out=xh_out[i],
+                                  dT_out=dT_out[i], device=dev)
+            radii += r["n_radii"]
+        return radii
+
+    for _ in range(3):
+        step()
+    barrier()
+    t0 = time.perf_counter()
+    radii = 0
+    for _ in range(args.steps):
+        radii += step()
+    barrier()
+    dt = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([dt], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+    world = dist.get_world_size() if dist is not None else 1
+    nb = len(work)
+    return {"value": N ** 3 * radii * world / dt, "unit": UNIT, "h2d_bytes_per_step": nb * N ** 3 * 4,
+            "d2h_bytes_per_step": nb * (2 * N ** 3 * 4 + 3 * NUM_BINS * 4 + 8),
+            "api": "Programs.pipeline.simulate_box (find_HII_bubbles + delta_T on pinned host buffers)",
+            "ms_per_step": 1e3 * dt / args.steps}
+
+
+def measured_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if there is one."""
+    path = os.path.join(ROOT, "profiles", "traffic_256.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) >= 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel:
+                    return float(parts[2])
+    except OSError:
+        pass
+    return None
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -93,6 +93,30 @@ int es_power_spectrum(es_plan* plan, const float* dT, const float* ave, const in
 int es_fft_r2c(es_plan* plan, const float* in, void* out_half, void* stream);
 int es_fft_c2r(es_plan* plan, const void* in_half, float* out, void* stream);
 
+/* Per-launch timing.  es_profile_enable(plan, K) pre-creates event pairs for K launches (0
+ * turns timing off); every kernel the plan launches afterwards is bracketed by CUDA events on
+ * its stream.  es_profile_read synchronises on the recorded events and writes, per kernel kind
+ * (ES_PROF_*), the summed milliseconds and launch counts; it returns the number of launches
+ * that found the pool full.  es_profile_reset starts a new window. */
+#define ES_PROF_COL_Z_FWD 0
+#define ES_PROF_COL_Y_FWD 1
+#define ES_PROF_COL_Z_INV_FILTER 2
+#define ES_PROF_COL_Y_INV 3
+#define ES_PROF_COL_Z_FWD_PK 4
+#define ES_PROF_ROW_R2C 5
+#define ES_PROF_ROW_R2C_PK 6
+#define ES_PROF_ROW_C2R 7
+#define ES_PROF_ROW_C2R_IONIZE 8
+#define ES_PROF_COL_Z_INV 9
+#define ES_PROF_FILTER_TABLE 10
+#define ES_PROF_FINAL 11
+#define ES_PROF_DELTA_T 12
+#define ES_PROF_PAINT 13
+#define ES_PROF_COUNT 14
+int es_profile_enable(es_plan* plan, int max_launches);
+int es_profile_reset(es_plan* plan);
+int es_profile_read(es_plan* plan, float* total_ms, int* counts, int nops);
+
 /* Message of the calling thread's last failure, copied into buf (NUL-terminated). */
 int es_last_error(char* buf, int len);
 int es_version(void);
