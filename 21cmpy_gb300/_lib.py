@@ -53,6 +53,7 @@ _PROTOS = {
     "es_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "es_ionize": (C.c_int, [C.c_void_p, C.POINTER(es_ionize_params), C.c_void_p, C.c_void_p, C.c_void_p]),
     "es_delta_T": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "es_delta_T_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
     "es_power_spectrum": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_int,
                                     C.c_void_p, C.c_void_p]),
     "es_fft_r2c": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

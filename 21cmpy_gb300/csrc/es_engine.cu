@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -652,6 +653,56 @@ int es_fft_c2r(es_plan* p, const void* in, float* out, void* stream) {
   a.cin = p->T;
   a.rout = reinterpret_cast<float2*>(out);
   return run_op(p, es::OP_ROW_C2R_STORE, a, grid_row(p), s);
+}
+
+// ------------------------------------------------------------------ allocation-free delta_T
+// Scratch of es_delta_T_noalloc: one partial sum per CTA (at most ES_NOALLOC_MAX_CTAS) and, in
+// the word after them, the CTAs' arrival counter.  It is a static device array, so every GPU that
+// loads this library holds these 16.25 KiB until the process exits, and every call shares it.
+static __device__ __align__(256) float g_noalloc_scratch[ES_NOALLOC_MAX_CTAS + 64];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kNoallocMaxDevices = 64;
+void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+int g_noalloc_grid[kNoallocMaxDevices] = {};
+}  // namespace
+
+int es_delta_T_noalloc(int n, const float* xH, const float* delta, float c, float* dT, float* ave, void* stream) {
+  if (!xH || !delta || !dT || !ave) return fail(ES_E_ARG, "es_delta_T_noalloc: NULL argument");
+  if (n < 2 || n % 2 || n > ES_NOALLOC_MAX_N)
+    return fail(ES_E_ARG, "es_delta_T_noalloc: HII_DIM=%d must be even and at most %d", n, ES_NOALLOC_MAX_N);
+  int dev = 0;
+  ES_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoallocMaxDevices) return fail(ES_E_ARG, "es_delta_T_noalloc: device %d out of range", dev);
+  void* base = nullptr;
+  int grid = 0;
+  {
+    // first call on this device: resolve the device address of the static scratch (host code
+    // cannot use the array's name as a device pointer) and size the grid to the device
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* ptr = nullptr;
+      ES_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+      int sms = 0;
+      ES_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      g_noalloc_grid[dev] = sms * 8 < ES_NOALLOC_MAX_CTAS ? sms * 8 : ES_NOALLOC_MAX_CTAS;
+      g_noalloc_ptr[dev] = ptr;
+    }
+    base = g_noalloc_ptr[dev];
+    grid = g_noalloc_grid[dev];
+  }
+  float* partials = static_cast<float*>(base);
+  unsigned* counter = reinterpret_cast<unsigned*>(partials + ES_NOALLOC_MAX_CTAS);
+  cudaStream_t s = (cudaStream_t)stream;
+  // the counter must start at zero; a call that never finished would have left it elsewhere
+  ES_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), s));
+  const size_t N3 = (size_t)n * n * n;
+  delta_T_kernel<256><<<grid, 256, 0, s>>>(
+      reinterpret_cast<const float2*>(xH), reinterpret_cast<const float2*>(delta), (long)(N3 / 2), c,
+      reinterpret_cast<float2*>(dT), partials, counter, ave, (float)(1.0 / (double)N3));
+  ES_CUDA(cudaGetLastError());
+  return ES_OK;
 }
 
 int es_profile_enable(es_plan* p, int max_launches) {

@@ -79,6 +79,21 @@ int es_ionize(es_plan* plan, const es_ionize_params* params, float* out, float* 
 int es_delta_T(es_plan* plan, const float* xH, const float* delta, float const_factor,
                float* dT, float* ave, void* stream);
 
+/* es_delta_T without a plan and without allocating anything: for callers that cannot call
+ * cudaMalloc, such as code running inside another runtime's memory pool, host code that is
+ * only handed device pointers, or embedders that forbid allocation after start-up.  No
+ * counterpart in the reference.  The mean's partial sums live in a static device array of
+ * ES_NOALLOC_MAX_CTAS + 64 floats (16.25 KiB) that every GPU loading the library keeps until
+ * exit.  The first call on a device looks up that array's device address (cudaGetSymbolAddress)
+ * with the device current; make that first call before any stream capture.  Every call shares
+ * the array, so calls that overlap on the GPU (other streams, other threads) race: serialise
+ * them.  n: even HII_DIM up to ES_NOALLOC_MAX_N; other arguments as es_delta_T, on the
+ * current device. */
+#define ES_NOALLOC_MAX_CTAS 4096
+#define ES_NOALLOC_MAX_N 1024
+int es_delta_T_noalloc(int n, const float* xH, const float* delta, float const_factor,
+                       float* dT, float* ave, void* stream);
+
 /* Spherically binned power spectrum of g = (dT / ave - 1) V / n^3 (times ave when
  * dimensional), the intended pbox_kernel (delta_T.cu:5-29, delta_T.py:80-98).
  * k2_thresholds: host int[nbins], a mode of integer |k/dk|^2 = m goes to the first bin b
