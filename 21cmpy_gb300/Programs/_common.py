@@ -59,6 +59,8 @@ def plan_for(n: int, box_len: float, max_radii: int, device):
         if plan is not None:
             _plans.pop(key).close()
         plan = ExcursionSetPlan(n, box_len, max_radii=max(64, max_radii), device=dev)
+        from ..autotune import ensure_tuned
+        ensure_tuned(plan)
         _plans[key] = plan
         while len(_plans) > MAX_CACHED_PLANS:
             _plans.popitem(last=False)[1].close()

@@ -17,7 +17,11 @@ ES_OK = 0
 PROF_KINDS = ("col_z_fwd", "col_y_fwd", "col_z_inv_filter", "col_y_inv", "col_z_fwd_pk", "row_r2c",
               "row_r2c_pk", "row_c2r", "row_c2r_ionize", "col_z_inv", "filter_table", "final",
               "delta_T", "paint")
-ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "unsupported box size"}
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "unsupported box size",
+          -5: "device-side wait timed out"}
+OPT_COL_VARIANT = 1
+OPT_COL_TILE = 2
+OPT_ROW_TILE = 3
 
 
 class EngineUnavailable(RuntimeError):
@@ -50,6 +54,9 @@ _PROTOS = {
     "es_plan_destroy": (C.c_int, [C.c_void_p]),
     "es_plan_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int]),
     "es_supported_sizes": (C.c_int, [C.POINTER(C.c_int), C.c_int]),
+    "es_plan_set_option": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "es_plan_get_option": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "es_plan_check": (C.c_int, [C.c_void_p, C.c_void_p]),
     "es_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "es_ionize": (C.c_int, [C.c_void_p, C.POINTER(es_ionize_params), C.c_void_p, C.c_void_p, C.c_void_p]),
     "es_delta_T": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -61,6 +68,7 @@ _PROTOS = {
     "es_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
     "es_profile_reset": (C.c_int, [C.c_void_p]),
     "es_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_int]),
+    "es_selftest_erfc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_version": (C.c_int, []),
 }

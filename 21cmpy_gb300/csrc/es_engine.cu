@@ -1,6 +1,8 @@
 // Host engine and C ABI of the excursion-set path (declared in include/es_engine.h), plus the
 // size-independent kernels: filter tables, final partial ionisation, sphere painting, delta_T
 // and layout conversions for the FFT self-tests.
+#include <cudaTypedefs.h>
+
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -86,7 +88,7 @@ struct es_plan {
   uint32_t* centers = nullptr;
   float* wtab = nullptr;
   float* partials = nullptr;
-  unsigned* counters = nullptr;     // [0] reductions, [1] centre count
+  unsigned* counters = nullptr;     // [0] reductions, [1] centre count, [2] error word
   float* stats = nullptr;           // [max_radii + 2][4]
   RadDev* rad = nullptr;
   int* thr = nullptr;
@@ -100,6 +102,11 @@ struct es_plan {
   std::vector<int> prof_ops;
   int prof_used = 0;
   int prof_dropped = 0;
+  // TMA descriptors: main arrays with z-pass and y-pass boxes, Nyquist planes with z-pass boxes
+  CUtensorMap tmX_z, tmX_y, tmXn, tmT_z, tmT_y, tmTn;
+  int col_variant = 1;              // passes: 1 TMA double-buffered (default), 0 synchronous
+  int col_tile = 0, row_tile = 0;   // TMA tile-shape variants
+  unsigned* err = nullptr;          // device error word (timed-out waits)
 };
 
 namespace {
@@ -157,19 +164,6 @@ size_t partial_floats_for(int sms, const es::OpGeometry& g) {
 
 // ------------------------------------------------------------------ size-independent kernels
 
-__device__ __forceinline__ float rtophat_f(float x) {
-  // W(x) = 3 (sin x - x cos x) / x^3; its Taylor series sum_n 3 (-1)^n (2n+2) x^(2n) / (2n+3)!
-  // below x = 1 avoids the cancellation of the closed form
-  if (x < 1.0f) {
-    const float y = x * x;
-    return 1.0f + y * (-0.1f + y * (1.0f / 280.0f + y * (-1.0f / 15120.0f +
-           y * (1.0f / 1330560.0f + y * (-1.0f / 172972800.0f)))));
-  }
-  float s, c;
-  sincosf(x, &s, &c);
-  return 3.0f * (s - x * c) / (x * x * x);
-}
-
 __global__ void filter_table_kernel(float* wtab, int k2n, const RadDev* rad, int nr, float dk,
                                     int filter, int ref_compat, float inv_n3) {
   const long total = (long)nr * k2n;
@@ -177,20 +171,7 @@ __global__ void filter_table_kernel(float* wtab, int k2n, const RadDev* rad, int
        idx += (long)gridDim.x * blockDim.x) {
     const int r = (int)(idx / k2n), k2 = (int)(idx % k2n);
     const RadDev rd = rad[r];
-    const float kR = dk * sqrtf((float)k2) * rd.R;
-    float W;
-    if (!ref_compat) {
-      if (filter == 0) W = rtophat_f(kR);
-      else if (filter == 1) W = k2 <= rd.k2cut ? 1.0f : 0.0f;
-      else { const float x = 0.643f * kR; W = expf(-0.5f * x * x); }
-    } else {   // find_bubbles.cu:28-41, switch without break
-      W = 1.0f;
-      float x = kR;
-      if (filter == 0 && kR > 1e-4f) W = rtophat_f(kR);
-      if (filter <= 1) { x *= 0.413566994f; if (k2 > rd.k2cut) W = 0.0f; }
-      x *= 0.643f;
-      W *= expf(-0.5f * x * x);
-    }
+    const float W = es::filter_weight(k2, dk, rd.R, rd.k2cut, filter, ref_compat);
     wtab[idx] = W * inv_n3;
   }
 }
@@ -206,13 +187,13 @@ __global__ void __launch_bounds__(T) final_kernel(const float2* dR, const uint32
   float acc = 0.f;
   for (long p = blockIdx.x * (long)T + threadIdx.x; p < pairs; p += (long)gridDim.x * T) {
     const float2 d = dR[p];
-    const uint32_t w = __ldg(flags + (p * 2) / 32);
-    const int bit = (int)((p * 2) % 32);
+    const unsigned long long w = __ldg(reinterpret_cast<const unsigned long long*>(flags) + p / 32);
+    const int bit = (int)(p % 32);
     float ion[2];
     const float dv[2] = {d.x, d.y};
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      if ((w >> (bit + h)) & 1u) { ion[h] = 1.0f; continue; }
+      if ((w >> (bit + 32 * h)) & 1ull) { ion[h] = 1.0f; continue; }
       const float f = erfcf((dc - dv[h]) / denom) * norm;
       ion[h] = f >= inv_zeta ? 1.0f : f * zeta;        // final_kernel (find_bubbles.cu:150-157)
     }
@@ -246,13 +227,25 @@ __device__ __forceinline__ int isqrt_dev(int v) {
   return r;
 }
 
+__device__ __forceinline__ unsigned long long bit_range(long lo, long hi, long q) {
+  // bits lo - 32q .. hi - 32q of a 32-bit half, clipped to [0, 31]; 0 when empty
+  if (lo < 32 * q) lo = 32 * q;
+  if (hi > 32 * q + 31) hi = 32 * q + 31;
+  if (lo > hi) return 0ull;
+  const int l = (int)(lo - 32 * q), h = (int)(hi - 32 * q);
+  const unsigned long long top = h == 31 ? 0xffffffffull : ((1ull << (h + 1)) - 1ull);
+  return top & ~((1ull << l) - 1ull);
+}
+
+// set voxels a..b (inclusive) in the pair-major bitmap: voxel v = 2p + h is bit (p % 32) + 32 h
+// of 64-bit word p / 32
 __device__ __forceinline__ void set_bits(uint32_t* flags, long a, long b) {
-  // set bits a..b (inclusive) of the flag bitmap
-  for (long w = a / 32; w <= b / 32; ++w) {
-    const int lo = (int)((a > w * 32 ? a : w * 32) - w * 32);
-    const int hi = (int)((b < w * 32 + 31 ? b : w * 32 + 31) - w * 32);
-    const uint32_t himask = hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u);
-    atomicOr(flags + w, himask & ~((1u << lo) - 1u));
+  unsigned long long* f = reinterpret_cast<unsigned long long*>(flags);
+  const long e_lo = (a + 1) >> 1, e_hi = b >> 1;          // even voxels 2p in [a, b]
+  const long o_lo = a >> 1, o_hi = (b - 1) >> 1;          // odd voxels 2p + 1 in [a, b]
+  for (long q = (a >> 1) / 32; q <= (b >> 1) / 32; ++q) {
+    const unsigned long long m = bit_range(e_lo, e_hi, q) | (bit_range(o_lo, o_hi, q) << 32);
+    if (m) atomicOr(f + q, m);
   }
 }
 
@@ -292,6 +285,13 @@ __global__ void paint_kernel(const uint32_t* centers, const unsigned* count, uin
   }
 }
 
+__global__ void erfc_selftest_kernel(const float* x, float* fast, float* lib, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    fast[i] = es::erfc_sum_term(x[i]);
+    lib[i] = erfcf(x[i]);
+  }
+}
+
 // numpy rfftn layout (n, n, n/2+1)  <->  main (n, n, n/2) + nyq (n, n)
 __global__ void to_std_kernel(const float2* mainp, const float2* nyq, float2* out, int n) {
   const int m = n / 2;
@@ -313,14 +313,82 @@ __global__ void from_std_kernel(const float2* in, float2* mainp, float2* nyq, in
   }
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+// main spectrum [k][j][i < n/2] as 8-byte elements; z-pass box (ti, 1, box), y-pass box (ti, box, 1)
+int make_main_map(CUtensorMap* m, void* base, int n, int ti, bool zbox) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return fail(ES_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  const cuuint64_t M = n / 2;
+  const cuuint32_t box = n < 256 ? n : 256;
+  cuuint64_t dims[3] = {M, (cuuint64_t)n, (cuuint64_t)n};
+  cuuint64_t strides[2] = {M * 8, (cuuint64_t)n * M * 8};
+  cuuint32_t bdim[3] = {(cuuint32_t)ti, zbox ? 1u : box, zbox ? box : 1u};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, bdim, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ES_E_CUDA, "cuTensorMapEncodeTiled (main, n=%d) failed: %d", n, (int)r);
+  return ES_OK;
+}
+
+// Nyquist plane [k][j] as 8-byte elements; box (ti, box)
+int make_nyq_map(CUtensorMap* m, void* base, int n, int ti) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return fail(ES_E_CUDA, "cuTensorMapEncodeTiled is unavailable");
+  const cuuint32_t box = n < 256 ? n : 256;
+  cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+  cuuint64_t strides[1] = {(cuuint64_t)n * 8};
+  cuuint32_t bdim[2] = {(cuuint32_t)ti, box};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, base, dims, strides, bdim, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ES_E_CUDA, "cuTensorMapEncodeTiled (nyq, n=%d) failed: %d", n, (int)r);
+  return ES_OK;
+}
+
+// TMA descriptors of the plan's spectra for the current column tile width
+int encode_maps(es_plan* p) {
+  int rc = 0;
+  const int n = p->n, ti = p->geo.tcol_ti[p->col_tile];
+  if ((rc = make_main_map(&p->tmX_z, p->X, n, ti, true)) || (rc = make_main_map(&p->tmX_y, p->X, n, ti, false)) ||
+      (rc = make_main_map(&p->tmT_z, p->T, n, ti, true)) || (rc = make_main_map(&p->tmT_y, p->T, n, ti, false)) ||
+      (rc = make_nyq_map(&p->tmXn, p->Xnyq, n, ti)) || (rc = make_nyq_map(&p->tmTn, p->Tnyq, n, ti)))
+    return rc;
+  return ES_OK;
+}
+
 es::OpArgs base_args(const es_plan* p) {
   es::OpArgs a;
   std::memset(&a, 0, sizeof(a));
   a.tw = p->tw;
   a.partials = p->partials;
   a.counter = p->counters;
+  a.err = p->err;
+  a.variant = p->col_variant;
+  a.col_tile = p->col_tile;
+  a.row_tile = p->row_tile;
   a.scale = 1.0f;
   return a;
+}
+
+// column-pass descriptors: input / output spectra, Nyquist planes, for a z or a y pass
+void set_maps(es::OpArgs& a, const CUtensorMap& in, const CUtensorMap& out, const CUtensorMap* in_nyq,
+              const CUtensorMap* out_nyq) {
+  a.tm_in = in;
+  a.tm_out = out;
+  if (in_nyq) a.tm_in_nyq = *in_nyq;
+  if (out_nyq) a.tm_out_nyq = *out_nyq;
 }
 
 // Records the start event of a timed launch; returns the slot or -1 when timing is off/full.
@@ -346,10 +414,28 @@ int run_op(es_plan* p, int op, es::OpArgs a, int grid, cudaStream_t s) {
 }
 
 int grid_col_z(const es_plan* p, bool pk) {
+  if (p->col_variant == 1) {
+    const int v = p->col_tile;
+    return occupancy_grid(p, p->geo.tcol_tiles_z[v], p->geo.tcol_threads[v],
+                          pk ? p->geo.tcol_smem_pk[v] : p->geo.tcol_smem[v]);
+  }
   return occupancy_grid(p, p->geo.col_tiles_z, p->geo.col_threads, pk ? p->geo.col_smem_pk : p->geo.col_smem);
 }
-int grid_col_y(const es_plan* p) { return occupancy_grid(p, p->geo.col_tiles_y, p->geo.col_threads, p->geo.col_smem); }
-int grid_row(const es_plan* p) { return occupancy_grid(p, p->geo.row_tiles, p->geo.row_threads, p->geo.row_smem); }
+int grid_col_y(const es_plan* p) {
+  if (p->col_variant == 1) {
+    const int v = p->col_tile;
+    return occupancy_grid(p, p->geo.tcol_tiles_y[v], p->geo.tcol_threads[v], p->geo.tcol_smem[v]);
+  }
+  return occupancy_grid(p, p->geo.col_tiles_y, p->geo.col_threads, p->geo.col_smem);
+}
+int grid_row(const es_plan* p, bool prev = false) {
+  if (p->col_variant == 1) {
+    const int v = p->row_tile;
+    return occupancy_grid(p, p->geo.trow_tiles[v], p->geo.trow_threads[v],
+                          prev ? p->geo.trow_smem_prev[v] : p->geo.trow_smem[v]);
+  }
+  return occupancy_grid(p, p->geo.row_tiles, p->geo.row_threads, p->geo.row_smem);
+}
 int grid_elem(const es_plan* p) { return p->sms * 8; }
 
 // wait until the previous upload from the staging buffers has been consumed
@@ -359,8 +445,13 @@ int reuse_staging(es_plan* p) {
   return ES_OK;
 }
 
-// forward transform of a real box into (mainp, nyq); rows -> y -> z
-int forward_into(es_plan* p, const float* in, float scale, float2* mainp, float2* nyq, cudaStream_t s) {
+// forward transform of a real box into the X (into_T = false) or T spectrum; rows -> y -> z
+int forward_into(es_plan* p, const float* in, float scale, bool into_T, cudaStream_t s) {
+  float2* mainp = into_T ? p->T : p->X;
+  float2* nyq = into_T ? p->Tnyq : p->Xnyq;
+  const CUtensorMap& mz = into_T ? p->tmT_z : p->tmX_z;
+  const CUtensorMap& my = into_T ? p->tmT_y : p->tmX_y;
+  const CUtensorMap& mn = into_T ? p->tmTn : p->tmXn;
   es::OpArgs a = base_args(p);
   a.rin = reinterpret_cast<const float2*>(in);
   a.cout = mainp;
@@ -369,9 +460,11 @@ int forward_into(es_plan* p, const float* in, float scale, float2* mainp, float2
   if (rc) return rc;
   a = base_args(p);
   a.cin = mainp; a.cout = mainp; a.cout_nyq = nyq;
+  set_maps(a, my, my, nullptr, nullptr);
   if ((rc = run_op(p, es::OP_COL_Y_FWD, a, grid_col_y(p), s))) return rc;
   a = base_args(p);
   a.cin = mainp; a.cin_nyq = nyq; a.cout = mainp; a.cout_nyq = nyq;
+  set_maps(a, mz, mz, &mn, &mn);
   return run_op(p, es::OP_COL_Z_FWD, a, grid_col_z(p, false), s);
 }
 
@@ -443,6 +536,8 @@ int es_plan_create(int n, double box_len, int max_radii, es_plan** out) {
   p->stats = (float*)(b + L.stats);
   p->rad = (RadDev*)(b + L.rad);
   p->thr = (int*)(b + L.thr);
+  p->err = p->counters + 2;
+  if (int rc = encode_maps(p)) return cleanup(rc);
   if (cudaMallocHost(&p->h_rad, sizeof(RadDev) * max_radii) != cudaSuccess ||
       cudaMallocHost(&p->h_thr, sizeof(int) * es::PK_MAX_BINS) != cudaSuccess)
     return cleanup(fail(ES_E_NOMEM, "es_plan_create: pinned staging allocation failed"));
@@ -479,7 +574,7 @@ int es_plan_destroy(es_plan* p) {
 int es_forward(es_plan* p, const float* delta, void* stream) {
   if (!p || !delta) return fail(ES_E_ARG, "es_forward: NULL argument");
   DeviceGuard g(p->device);
-  return forward_into(p, delta, 1.0f, p->X, p->Xnyq, (cudaStream_t)stream);
+  return forward_into(p, delta, 1.0f, false, (cudaStream_t)stream);
 }
 
 int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, void* stream) {
@@ -527,11 +622,14 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
   ES_CUDA(cudaMemcpyAsync(p->rad, p->h_rad, sizeof(RadDev) * nr, cudaMemcpyHostToDevice, s));
   ES_CUDA(cudaEventRecord(p->staged, s));
   const float inv_n3 = (float)(1.0 / ((double)p->n * p->n * p->n));
-  int slot = prof_begin(p, ES_PROF_FILTER_TABLE, s);
-  filter_table_kernel<<<p->sms * 4, 256, 0, s>>>(p->wtab, p->k2n, p->rad, nr, p->dk, prm->filter_type,
-                                                   prm->ref_compat, inv_n3);
-  prof_end(p, slot, s);
-  ES_CUDA(cudaGetLastError());
+  int slot = -1;
+  if (p->col_variant == 0) {        // the synchronous column pass gathers W from per-radius tables
+    slot = prof_begin(p, ES_PROF_FILTER_TABLE, s);
+    filter_table_kernel<<<p->sms * 4, 256, 0, s>>>(p->wtab, p->k2n, p->rad, nr, p->dk, prm->filter_type,
+                                                     prm->ref_compat, inv_n3);
+    prof_end(p, slot, s);
+    ES_CUDA(cudaGetLastError());
+  }
   const size_t N3 = (size_t)p->n * p->n * p->n;
   ES_CUDA(cudaMemsetAsync(p->flags, 0, N3 / 8, s));
   const float inv_zeta = (float)(1.0 / (double)prm->zeta);
@@ -540,9 +638,17 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     a.cin = p->X; a.cin_nyq = p->Xnyq; a.cout = p->T; a.cout_nyq = p->Tnyq;
     a.wtab = p->wtab + (size_t)r * p->k2n;
     a.scale = prm->growth_scale;
+    a.fR = p->h_rad[r].R;
+    a.fk2cut = p->h_rad[r].k2cut;
+    a.filter = prm->filter_type;
+    a.ref_compat = prm->ref_compat;
+    a.dk = p->dk;
+    a.inv_n3 = inv_n3;
+    set_maps(a, p->tmX_z, p->tmT_z, &p->tmXn, &p->tmTn);
     if ((rc = run_op(p, es::OP_COL_Z_INV_FILTER, a, grid_col_z(p, false), s))) return rc;
     a = base_args(p);
     a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T;
+    set_maps(a, p->tmT_y, p->tmT_y, nullptr, nullptr);
     if ((rc = run_op(p, es::OP_COL_Y_INV, a, grid_col_y(p), s))) return rc;
     if (prm->update == 1 && r > 0) ES_CUDA(cudaMemsetAsync(p->counters + 1, 0, sizeof(unsigned), s));
     a = base_args(p);
@@ -562,7 +668,7 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     a.center_count = p->counters + 1;
     a.fc_mean = prm->fc_mean_ps;
     a.normalize = prm->normalize_mean;
-    if ((rc = run_op(p, es::OP_ROW_C2R_IONIZE, a, grid_row(p), s))) return rc;
+    if ((rc = run_op(p, es::OP_ROW_C2R_IONIZE, a, grid_row(p, true), s))) return rc;
     if (prm->update == 1 && r > 0) {
       slot = prof_begin(p, ES_PROF_PAINT, s);
       paint_kernel<<<p->sms * 4, 256, 0, s>>>(p->centers, p->counters + 1, p->flags, p->n,
@@ -617,9 +723,11 @@ int es_power_spectrum(es_plan* p, const float* dT, const float* ave, const int* 
   if ((rc = run_op(p, es::OP_ROW_R2C_PK, a, grid_row(p), s))) return rc;
   a = base_args(p);
   a.cin = p->T; a.cout = p->T; a.cout_nyq = p->Tnyq;
+  set_maps(a, p->tmT_y, p->tmT_y, nullptr, nullptr);
   if ((rc = run_op(p, es::OP_COL_Y_FWD, a, grid_col_y(p), s))) return rc;
   a = base_args(p);
   a.cin = p->T; a.cin_nyq = p->Tnyq;
+  set_maps(a, p->tmT_z, p->tmT_z, &p->tmTn, &p->tmTn);
   a.thr = p->thr; a.nbins = nbins; a.dk = p->dk; a.volume = (float)(L * L * L);
   a.pk_out = out;
   return run_op(p, es::OP_COL_Z_FWD_PK, a, grid_col_z(p, true), s);
@@ -629,7 +737,7 @@ int es_fft_r2c(es_plan* p, const float* in, void* out, void* stream) {
   if (!p || !in || !out) return fail(ES_E_ARG, "es_fft_r2c: NULL argument");
   DeviceGuard g(p->device);
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = forward_into(p, in, 1.0f, p->T, p->Tnyq, s);
+  int rc = forward_into(p, in, 1.0f, true, s);
   if (rc) return rc;
   to_std_kernel<<<p->sms * 8, 256, 0, s>>>(p->T, p->Tnyq, (float2*)out, p->n);
   ES_CUDA(cudaGetLastError());
@@ -644,10 +752,12 @@ int es_fft_c2r(es_plan* p, const void* in, float* out, void* stream) {
   ES_CUDA(cudaGetLastError());
   es::OpArgs a = base_args(p);
   a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T; a.cout_nyq = p->Tnyq;
+  set_maps(a, p->tmT_z, p->tmT_z, &p->tmTn, &p->tmTn);
   int rc = run_op(p, es::OP_COL_Z_INV, a, grid_col_z(p, false), s);
   if (rc) return rc;
   a = base_args(p);
   a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T;
+  set_maps(a, p->tmT_y, p->tmT_y, nullptr, nullptr);
   if ((rc = run_op(p, es::OP_COL_Y_INV, a, grid_col_y(p), s))) return rc;
   a = base_args(p);
   a.cin = p->T;
@@ -702,6 +812,60 @@ int es_delta_T_noalloc(int n, const float* xH, const float* delta, float c, floa
       reinterpret_cast<const float2*>(xH), reinterpret_cast<const float2*>(delta), (long)(N3 / 2), c,
       reinterpret_cast<float2*>(dT), partials, counter, ave, (float)(1.0 / (double)N3));
   ES_CUDA(cudaGetLastError());
+  return ES_OK;
+}
+
+int es_selftest_erfc(const float* x, float* fast, float* lib, int n, void* stream) {
+  if (!x || !fast || !lib || n < 0) return fail(ES_E_ARG, "es_selftest_erfc: bad arguments");
+  if (n == 0) return ES_OK;
+  erfc_selftest_kernel<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, (cudaStream_t)stream>>>(x, fast, lib, n);
+  ES_CUDA(cudaGetLastError());
+  return ES_OK;
+}
+
+int es_plan_set_option(es_plan* p, int option, int value) {
+  if (!p) return fail(ES_E_ARG, "es_plan_set_option: NULL plan");
+  switch (option) {
+    case ES_OPT_COL_VARIANT:
+      if (value != 0 && value != 1) return fail(ES_E_ARG, "es_plan_set_option: column variant must be 0 or 1");
+      p->col_variant = value;
+      return ES_OK;
+    case ES_OPT_COL_TILE: {
+      if (value < 0 || value >= es::kColTileVariants) return fail(ES_E_ARG, "es_plan_set_option: column tile variant out of range");
+      const int old = p->col_tile;
+      p->col_tile = value;
+      if (int rc = encode_maps(p)) { p->col_tile = old; encode_maps(p); return rc; }
+      return ES_OK;
+    }
+    case ES_OPT_ROW_TILE:
+      if (value < 0 || value >= es::kRowTileVariants) return fail(ES_E_ARG, "es_plan_set_option: row tile variant out of range");
+      p->row_tile = value;
+      return ES_OK;
+    default:
+      return fail(ES_E_ARG, "es_plan_set_option: unknown option %d", option);
+  }
+}
+
+int es_plan_get_option(es_plan* p, int option, int* value) {
+  if (!p || !value) return fail(ES_E_ARG, "es_plan_get_option: NULL argument");
+  switch (option) {
+    case ES_OPT_COL_VARIANT: *value = p->col_variant; return ES_OK;
+    case ES_OPT_COL_TILE: *value = p->col_tile; return ES_OK;
+    case ES_OPT_ROW_TILE: *value = p->row_tile; return ES_OK;
+    default: return fail(ES_E_ARG, "es_plan_get_option: unknown option %d", option);
+  }
+}
+
+int es_plan_check(es_plan* p, void* stream) {
+  if (!p) return fail(ES_E_ARG, "es_plan_check: NULL plan");
+  DeviceGuard g(p->device);
+  unsigned word = 0;
+  ES_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  ES_CUDA(cudaMemcpy(&word, p->err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (word) {
+    ES_CUDA(cudaMemset(p->err, 0, sizeof(unsigned)));
+    return fail(ES_E_DEVICE, "a device-side wait timed out (error word 0x%x); results of the affected calls are invalid", word);
+  }
   return ES_OK;
 }
 

@@ -1,6 +1,8 @@
 // Per-box-size instantiation of the FFT pass kernels.  Compiled once per supported N with
 // -DES_N=<N>; each object exports es_launch_<N>(), which es_engine.cu dispatches to.
 #include "es_kernels.cuh"
+#include "es_tma.cuh"
+#include "es_rows.cuh"
 #include "es_ops.h"
 
 #ifndef ES_N
@@ -27,32 +29,71 @@ static cudaError_t launch(int smem, const OpArgs& a, int threads, cudaStream_t s
   return cudaGetLastError();
 }
 
+template <int N, int MODE>
+static cudaError_t launch_col(const OpArgs& a, cudaStream_t s) {
+  if (a.variant == 0) return launch<col_pass<N, MODE>>(ColSmem<N, MODE>::bytes, a, ColCfg<N>::T, s);
+  if (a.col_tile == 1) return launch<col_tma<N, MODE, 1>>(TmaSmem<N, MODE, 1>::bytes, a, ColTile<N, 1>::T, s);
+  if (a.col_tile == 2) return launch<col_tma<N, MODE, 2>>(TmaSmem<N, MODE, 2>::bytes, a, ColTile<N, 2>::T, s);
+  return launch<col_tma<N, MODE, 0>>(TmaSmem<N, MODE, 0>::bytes, a, ColTile<N, 0>::T, s);
+}
+
+template <int N, int PRO>
+static cudaError_t launch_r2c(const OpArgs& a, cudaStream_t s) {
+  if (a.variant == 0) return launch<row_r2c<N, PRO>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
+  switch (a.row_tile) {
+    case 1: return launch<row2_r2c<N, PRO, 1>>(Row2Smem<N, false, 1>::bytes, a, RowTile<N, 1>::T, s);
+    case 2: return launch<row2_r2c<N, PRO, 2>>(Row2Smem<N, false, 2>::bytes, a, RowTile<N, 2>::T, s);
+    case 3: return launch<row2_r2c<N, PRO, 3>>(Row2Smem<N, false, 3>::bytes, a, RowTile<N, 3>::T, s);
+    default: return launch<row2_r2c<N, PRO, 0>>(Row2Smem<N, false, 0>::bytes, a, RowTile<N, 0>::T, s);
+  }
+}
+
+template <int N, int EPI>
+static cudaError_t launch_c2r(const OpArgs& a, cudaStream_t s) {
+  constexpr bool P = EPI == EPI_IONIZE;
+  if (a.variant == 0) return launch<row_c2r<N, EPI>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
+  switch (a.row_tile) {
+    case 1: return launch<row2_c2r<N, EPI, 1>>(Row2Smem<N, P, 1>::bytes, a, RowTile<N, 1>::T, s);
+    case 2: return launch<row2_c2r<N, EPI, 2>>(Row2Smem<N, P, 2>::bytes, a, RowTile<N, 2>::T, s);
+    case 3: return launch<row2_c2r<N, EPI, 3>>(Row2Smem<N, P, 3>::bytes, a, RowTile<N, 3>::T, s);
+    default: return launch<row2_c2r<N, EPI, 0>>(Row2Smem<N, P, 0>::bytes, a, RowTile<N, 0>::T, s);
+  }
+}
+
 template <int N>
 static cudaError_t launch_op(int op, const OpArgs& a, cudaStream_t s) {
   switch (op) {
-    case OP_COL_Z_FWD:
-      return launch<col_pass<N, COL_Z_FWD>>(ColSmem<N, COL_Z_FWD>::bytes, a, ColCfg<N>::T, s);
-    case OP_COL_Y_FWD:
-      return launch<col_pass<N, COL_Y_FWD>>(ColSmem<N, COL_Y_FWD>::bytes, a, ColCfg<N>::T, s);
-    case OP_COL_Z_INV_FILTER:
-      return launch<col_pass<N, COL_Z_INV_FILTER>>(ColSmem<N, COL_Z_INV_FILTER>::bytes, a, ColCfg<N>::T, s);
-    case OP_COL_Z_INV:
-      return launch<col_pass<N, COL_Z_INV>>(ColSmem<N, COL_Z_INV>::bytes, a, ColCfg<N>::T, s);
-    case OP_COL_Y_INV:
-      return launch<col_pass<N, COL_Y_INV>>(ColSmem<N, COL_Y_INV>::bytes, a, ColCfg<N>::T, s);
-    case OP_COL_Z_FWD_PK:
-      return launch<col_pass<N, COL_Z_FWD_PK>>(ColSmem<N, COL_Z_FWD_PK>::bytes, a, ColCfg<N>::T, s);
-    case OP_ROW_R2C_SCALE:
-      return launch<row_r2c<N, PRO_SCALE>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
-    case OP_ROW_R2C_PK:
-      return launch<row_r2c<N, PRO_PK>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
-    case OP_ROW_C2R_STORE:
-      return launch<row_c2r<N, EPI_STORE>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
-    case OP_ROW_C2R_IONIZE:
-      return launch<row_c2r<N, EPI_IONIZE>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
-    default:
-      return cudaErrorInvalidValue;
+    case OP_COL_Z_FWD: return launch_col<N, COL_Z_FWD>(a, s);
+    case OP_COL_Y_FWD: return launch_col<N, COL_Y_FWD>(a, s);
+    case OP_COL_Z_INV_FILTER: return launch_col<N, COL_Z_INV_FILTER>(a, s);
+    case OP_COL_Z_INV: return launch_col<N, COL_Z_INV>(a, s);
+    case OP_COL_Y_INV: return launch_col<N, COL_Y_INV>(a, s);
+    case OP_COL_Z_FWD_PK: return launch_col<N, COL_Z_FWD_PK>(a, s);
+    case OP_ROW_R2C_SCALE: return launch_r2c<N, PRO_SCALE>(a, s);
+    case OP_ROW_R2C_PK: return launch_r2c<N, PRO_PK>(a, s);
+    case OP_ROW_C2R_STORE: return launch_c2r<N, EPI_STORE>(a, s);
+    case OP_ROW_C2R_IONIZE: return launch_c2r<N, EPI_IONIZE>(a, s);
+    default: return cudaErrorInvalidValue;
   }
+}
+
+template <int N, int V>
+static void col_geometry(OpGeometry* g) {
+  constexpr int TI = ColTile<N, V>::TI;
+  g->tcol_ti[V] = TI;
+  g->tcol_threads[V] = ColTile<N, V>::T;
+  g->tcol_tiles_z[V] = N * ((N / 2) / TI) + N / TI;
+  g->tcol_tiles_y[V] = N * ((N / 2) / TI);
+  g->tcol_smem[V] = TmaSmem<N, COL_Z_INV_FILTER, V>::bytes;
+  g->tcol_smem_pk[V] = TmaSmem<N, COL_Z_FWD_PK, V>::bytes;
+}
+
+template <int N, int V>
+static void row_geometry(OpGeometry* g) {
+  g->trow_tiles[V] = N * N / RowTile<N, V>::RL;
+  g->trow_threads[V] = RowTile<N, V>::T;
+  g->trow_smem[V] = Row2Smem<N, false, V>::bytes;
+  g->trow_smem_prev[V] = Row2Smem<N, true, V>::bytes;
 }
 
 template <int N>
@@ -66,6 +107,13 @@ static void geometry(OpGeometry* g) {
   g->col_smem = ColSmem<N, COL_Z_INV_FILTER>::bytes;
   g->col_smem_pk = ColSmem<N, COL_Z_FWD_PK>::bytes;
   g->row_smem = RowSmem<N>::bytes;
+  col_geometry<N, 0>(g);
+  col_geometry<N, 1>(g);
+  col_geometry<N, 2>(g);
+  row_geometry<N, 0>(g);
+  row_geometry<N, 1>(g);
+  row_geometry<N, 2>(g);
+  row_geometry<N, 3>(g);
 }
 
 }  // namespace es

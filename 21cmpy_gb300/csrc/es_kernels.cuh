@@ -13,6 +13,7 @@
 // The i = 0 and i = N/2 columns are Hermitian in (j, k); along y they are transformed together
 // as one complex sequence (packed as re + i*im) and split again on the forward side.
 #pragma once
+#include <cuda.h>
 #include "es_fft.cuh"
 
 namespace es {
@@ -24,6 +25,11 @@ enum RowEpi { EPI_STORE = 0, EPI_IONIZE = 1 };
 constexpr int PK_MAX_BINS = 128;
 
 struct OpArgs {
+  // TMA descriptors of the column passes' input / output spectra (main array, Nyquist plane)
+  CUtensorMap tm_in, tm_out, tm_in_nyq, tm_out_nyq;
+  unsigned* err;                  // device error word (bounded waits that timed out)
+  int variant;                    // passes: 0 synchronous tiles, 1 TMA double-buffered
+  int col_tile, row_tile;         // TMA tile-shape variants (chosen by the autotuner)
   int grid;                       // CTAs to launch (persistent grid-stride)
   // real boxes viewed as float2 pairs of consecutive x
   const float2* rin;
@@ -40,10 +46,15 @@ struct OpArgs {
   float pk_norm;                  // PRO_PK: V / N^3
   int dimensional;                // PRO_PK: multiply by the mean (DIMENSIONAL_T_POWER_SPEC)
   // col-z inverse filter (times scale, the growth rescale)
-  const float* wtab;              // W(k^2) / N^3 for this radius
+  const float* wtab;              // W(k^2) / N^3 for this radius (synchronous variant)
+  float fR;                       // filter radius [Mpc] (TMA variant computes W inline)
+  int fk2cut;                     // k-space top-hat cut
+  int filter, ref_compat;
+  float inv_n3;
   // row C2R ionisation epilogue
   const float2* prev;             // delta_R of the previous radius (pairs)
-  uint32_t* flags;                // ionisation bits, bit v of word v/32
+  uint32_t* flags;                // ionisation bitmap, pair-major: voxel v = 2p + h is bit
+                                  // (p % 32) + 32 h of 64-bit word p / 32
   int has_prev;
   float dc;                       // delta_c(z) (float32, find_bubbles.cu:54)
   float denom;                    // this radius
@@ -109,6 +120,64 @@ __device__ __forceinline__ bool grid_sum(float mine, float* partials, unsigned* 
   if (threadIdx.x == 0) *counter = 0u;
   *total = acc;
   return true;
+}
+
+// erfc for the per-radius sum of fcoll, after Numerical Recipes' erfcc (Press et al. 1992, sec.
+// 6.2): erfc(z) = t exp(-z^2 - 1.26551223 + t P(t)), t = 1 / (1 + z/2), fractional error below
+// 1.2e-7 for z >= 0, erfc(-z) = 2 - erfc(z).  z^2 is split exactly (hi + lo, with an FMA) so
+// its rounding does not reach the exponential.  Only the sum over cells uses it; per-cell
+// values (final partial ionisation) use the library erfcf.
+__device__ __forceinline__ float erfc_sum_term(float x) {
+  const float z = fabsf(x);
+  const float t = 1.0f / fmaf(0.5f, z, 1.0f);
+  float p = 0.17087277f;
+  p = fmaf(p, t, -0.82215223f);
+  p = fmaf(p, t, 1.48851587f);
+  p = fmaf(p, t, -1.13520398f);
+  p = fmaf(p, t, 0.27886807f);
+  p = fmaf(p, t, -0.18628806f);
+  p = fmaf(p, t, 0.09678418f);
+  p = fmaf(p, t, 0.37409196f);
+  p = fmaf(p, t, 1.00002368f);
+  const float hi = z * z;
+  const float lo = fmaf(z, z, -hi);                    // z^2 = hi + lo exactly
+  // __expf is accurate to a few units of the last place for the arguments (|x| < 20) where
+  // erfc contributes to the sum
+  const float r = t * __expf(fmaf(t, p, -1.26551223f) - hi) * (1.0f - lo);
+  return x >= 0.0f ? r : 2.0f - r;
+}
+
+// Real-space top-hat W(x) = 3 (sin x - x cos x) / x^3; below x = 1 its Taylor series
+// sum_n 3 (-1)^n (2n+2) x^(2n) / (2n+3)! avoids the cancellation of the closed form.
+__device__ __forceinline__ float rtophat_f(float x) {
+  if (x < 1.0f) {
+    const float y = x * x;
+    return 1.0f + y * (-0.1f + y * (1.0f / 280.0f + y * (-1.0f / 15120.0f +
+           y * (1.0f / 1330560.0f + y * (-1.0f / 172972800.0f)))));
+  }
+  float s, c;
+  sincosf(x, &s, &c);
+  return 3.0f * (s - x * c) / (x * x * x);
+}
+
+// HII_filter's window (find_bubbles.cu:26-41) for a mode of integer |k/dk|^2 = k2.  k2cut is the
+// host-computed k-space top-hat cut; ref_compat reproduces the switch fall-through 0 -> 1 -> 2.
+__device__ __forceinline__ float filter_weight(int k2, float dk, float R, int k2cut, int filter, int ref_compat) {
+  const float kR = dk * sqrtf((float)k2) * R;
+  float W;
+  if (!ref_compat) {
+    if (filter == 0) W = rtophat_f(kR);
+    else if (filter == 1) W = k2 <= k2cut ? 1.0f : 0.0f;
+    else { const float x = 0.643f * kR; W = expf(-0.5f * x * x); }
+  } else {
+    W = 1.0f;
+    float x = kR;
+    if (filter == 0 && kR > 1e-4f) W = rtophat_f(kR);
+    if (filter <= 1) { x *= 0.413566994f; if (k2 > k2cut) W = 0.0f; }
+    x *= 0.643f;
+    W *= expf(-0.5f * x * x);
+  }
+  return W;
 }
 
 template <int N> __device__ __forceinline__ int wrap2(int k) {
@@ -374,10 +443,15 @@ __global__ void __launch_bounds__(RowCfg<N>::T) row_c2r(OpArgs a) {
   float2* B = A + RL * M;
   __shared__ float sred[T / 32];
   for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
-  float norm_prev = 1.f, inv_dp = 0.f;
-  if (EPI == EPI_IONIZE && a.has_prev) norm_prev = a.stats_prev[2];
-  const float dc = a.dc, denom = a.denom, dprev = a.denom_prev, izeta = a.inv_zeta;
-  (void)inv_dp;
+  // The previous radius' test erfc((dc - d) / denom_prev) * norm_prev >= 1/zeta is monotone in d:
+  // it holds exactly when d >= dc - denom_prev * erfcinv(1 / (zeta * norm_prev)), one scalar per
+  // radius instead of an erfc per cell.
+  float thr_prev = __int_as_float(0x7f800000);          // +inf: nothing passes
+  if (EPI == EPI_IONIZE && a.has_prev) {
+    const float y = a.inv_zeta / a.stats_prev[2];
+    if (y < 2.0f) thr_prev = a.dc - a.denom_prev * erfcinvf(y);
+  }
+  const float dc = a.dc, inv_denom = 1.0f / a.denom;
   float acc = 0.f;
   const int lane = threadIdx.x & 31;
   __syncthreads();
@@ -411,23 +485,17 @@ __global__ void __launch_bounds__(RowCfg<N>::T) row_c2r(OpArgs a) {
     } else {
       for (int e = threadIdx.x; e < RL * M; e += T) {   // whole warps: 64 consecutive voxels
         const float2 d = Zr[e];
-        acc += erfcf((dc - d.x) / denom) + erfcf((dc - d.y) / denom);
+        acc += erfcf((dc - d.x) * inv_denom) + erfcf((dc - d.y) * inv_denom);
         if (a.has_prev) {
           const float2 p = a.prev[base + e];
-          const bool px = erfcf((dc - p.x) / dprev) * norm_prev >= izeta;
-          const bool py = erfcf((dc - p.y) / dprev) * norm_prev >= izeta;
+          const bool px = p.x >= thr_prev;
+          const bool py = p.y >= thr_prev;
           const unsigned bx = __ballot_sync(0xffffffffu, px);
           const unsigned by = __ballot_sync(0xffffffffu, py);
           if (a.update == 0) {
-            if (lane < 2) {
-              const uint32_t bits = lane == 0
-                  ? (spread16(bx) | (spread16(by) << 1))
-                  : (spread16(bx >> 16) | (spread16(by >> 16) << 1));
-              if (bits) {
-                const size_t w = ((base + e - lane) * 2) / 32 + lane;
-                a.flags[w] |= bits;
-              }
-            }
+            if (lane == 0 && (bx | by))
+              atomicOr(reinterpret_cast<unsigned long long*>(a.flags) + (base + e) / 32,
+                       ((unsigned long long)by << 32) | bx);
           } else if (bx | by) {
             const unsigned cnt = __popc(bx) + __popc(by);
             unsigned first = 0;

@@ -19,10 +19,19 @@ enum Op {
   OP_COL_Z_INV = 9,
 };
 
+constexpr int kColTileVariants = 3;
+constexpr int kRowTileVariants = 4;
+
 struct OpGeometry {
   int col_tiles_z, col_tiles_y, row_tiles;
   int col_threads, row_threads;
   int col_smem, col_smem_pk, row_smem;
+  // TMA column passes, per tile variant (ES_OPT_COL_TILE)
+  int tcol_ti[kColTileVariants], tcol_threads[kColTileVariants], tcol_tiles_z[kColTileVariants];
+  int tcol_tiles_y[kColTileVariants], tcol_smem[kColTileVariants], tcol_smem_pk[kColTileVariants];
+  // TMA row passes, per tile variant (ES_OPT_ROW_TILE)
+  int trow_tiles[kRowTileVariants], trow_threads[kRowTileVariants], trow_smem[kRowTileVariants];
+  int trow_smem_prev[kRowTileVariants];
 };
 
 }  // namespace es

@@ -1,0 +1,264 @@
+// TMA-fed row passes (x axis): RL contiguous rows per tile arrive by 1-D bulk copies
+// (cp.async.bulk, two tiles in flight, completion on mbarriers), are transposed into a padded
+// [element][row] layout (pitch RL + 1, so every Stockham stage reads and writes shared memory
+// without bank conflicts) and leave through coalesced stores.
+#pragma once
+#include "es_tma.cuh"
+
+namespace es {
+
+template <int N> struct Row2Cfg;
+template <> struct Row2Cfg<32>  { static constexpr int RL = 16, T = 128; };
+template <> struct Row2Cfg<48>  { static constexpr int RL = 16, T = 128; };
+template <> struct Row2Cfg<64>  { static constexpr int RL = 16, T = 256; };
+template <> struct Row2Cfg<96>  { static constexpr int RL = 16, T = 256; };
+template <> struct Row2Cfg<128> { static constexpr int RL = 16, T = 256; };
+template <> struct Row2Cfg<160> { static constexpr int RL = 16, T = 256; };
+template <> struct Row2Cfg<256> { static constexpr int RL = 16, T = 256; };
+template <> struct Row2Cfg<512> { static constexpr int RL = 8,  T = 256; };
+
+// Row-pass tile shapes: variant 0 = (RL rows, T threads) above, 1 = RL/2 rows with T/2 threads,
+// 2 = RL rows with T/2 threads, 3 = RL rows with 2T threads.
+template <int N, int V> struct RowTile {
+  static constexpr int RL = V == 1 ? Row2Cfg<N>::RL / 2 : Row2Cfg<N>::RL;
+  static constexpr int T = V == 0 ? Row2Cfg<N>::T : (V == 3 ? 2 * Row2Cfg<N>::T : Row2Cfg<N>::T / 2);
+  static constexpr int MINB = T >= 512 ? 2 : 1;
+};
+
+template <int N, bool PREV, int V> struct Row2Smem {
+  static constexpr int RL = RowTile<N, V>::RL, M = N / 2;
+  static constexpr int stage = RL * M * 8;                 // one tile of rows, as loaded
+  static constexpr int work = M * (RL + 1) * 8;            // transposed, padded
+  // [S0 | S1 | P0 | P1 | A | B | twiddles | mbarriers] after aligning the base to 128 bytes
+  static constexpr int bytes = (PREV ? 4 : 2) * stage + 2 * work + N * 8 + 16 + 128;
+};
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Half-spectrum rows -> real rows with the excursion-set epilogue (EPI_IONIZE) or a plain store.
+template <int N, int EPI, int V>
+__global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2r(const __grid_constant__ OpArgs a) {
+  constexpr int M = N / 2, RL = RowTile<N, V>::RL, T = RowTile<N, V>::T, ES = RL + 1;
+  constexpr bool PREV = EPI == EPI_IONIZE;
+  using SM = Row2Smem<N, PREV, V>;
+  static_assert((RL * N) % 64 == 0 && (RL * M) % 32 == 0, "row tiles must hold whole 64-voxel flag pairs");
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  float2* const S0 = reinterpret_cast<float2*>(base);
+  float2* const S1 = reinterpret_cast<float2*>(base + SM::stage);
+  float2* const P0 = reinterpret_cast<float2*>(base + 2 * SM::stage);
+  float2* const P1 = reinterpret_cast<float2*>(base + 3 * SM::stage);
+  float2* A = reinterpret_cast<float2*>(base + (PREV ? 4 : 2) * SM::stage);
+  float2* B = A + M * ES;
+  float2* tw = B + M * ES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + N);
+  __shared__ float sred[T / 32];
+  __shared__ int s_abort;
+
+  const int ntiles = N * N / RL;
+  const int my_count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const bool has_prev = PREV && a.has_prev;
+  const uint32_t tile_bytes = RL * M * 8;
+  auto issue = [&](int it, int s) {
+    const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
+    mbar_expect_tx(&bars[s], has_prev ? 2 * tile_bytes : tile_bytes);
+    bulk_load(s ? S1 : S0, a.cin + pair0, tile_bytes, &bars[s]);
+    if (has_prev) bulk_load(s ? P1 : P0, a.prev + pair0, tile_bytes, &bars[s]);
+  };
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+    fence_async_smem();
+    for (int s = 0; s < 2 && s < my_count; ++s) issue(s, s);
+  }
+  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
+  // previous radius: erfc((dc - d) / denom_prev) * norm_prev >= 1/zeta  <=>  d >= thr_prev
+  float thr_prev = __int_as_float(0x7f800000);
+  if (has_prev) {
+    const float y = a.inv_zeta / a.stats_prev[2];
+    if (y < 2.0f) thr_prev = a.dc - a.denom_prev * erfcinvf(y);
+  }
+  const float dc = a.dc, inv_denom = PREV ? 1.0f / a.denom : 0.f;
+  const int lane = threadIdx.x & 31;
+  float acc = 0.f;
+  __syncthreads();
+
+  for (int it = 0; it < my_count; ++it) {
+    const int s = it & 1;
+    const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
+    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1))) {
+      atomicOr(a.err, ES_DEV_ERR_TIMEOUT);
+      s_abort = 1;
+    }
+    __syncthreads();
+    if (s_abort) break;
+    // C2R split + transpose: Z[m] = (X[m] + conj X[M-m]) + i w^-m (X[m] - conj X[M-m])
+    const float2* src = s ? S1 : S0;
+    for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += T) {
+      const int m = q % (M / 2 + 1), l = q / (M / 2 + 1);
+      const float2* x = src + l * M;
+      if (m == 0) {
+        const float2 x0 = x[0];                       // (X[0], X[N/2]), both real
+        A[l] = make_float2(x0.x + x0.y, x0.x - x0.y);
+      } else {
+        const int m2 = M - m;
+        const float2 xm = x[m], xc = x[m2];
+        const float2 t1 = cmul(cconj(tw[m]), make_float2(xm.x - xc.x, xm.y + xc.y));
+        A[m * ES + l] = make_float2(xm.x + xc.x - t1.y, xm.y - xc.y + t1.x);
+        if (m2 != m) {
+          const float2 t2 = cmul(cconj(tw[m2]), make_float2(xc.x - xm.x, xc.y + xm.y));
+          A[m2 * ES + l] = make_float2(xc.x + xm.x - t2.y, xc.y - xm.y + t2.x);
+        }
+      }
+    }
+    __syncthreads();
+    float2* Zr = fft_lines<M, true, RL, T, true, ES, 1, N>(A, B, tw);
+    if (EPI == EPI_STORE) {
+      for (int e = threadIdx.x; e < RL * M; e += T) {
+        const int row = e / M, p = e % M;
+        a.rout[pair0 + e] = Zr[p * ES + row];
+      }
+    } else {
+      const float2* pv = s ? P1 : P0;
+      for (int e = threadIdx.x; e < RL * M; e += T) {     // whole warps: 64 consecutive voxels
+        const int row = e / M, p = e % M;
+        const float2 d = Zr[p * ES + row];
+        acc += erfc_sum_term((dc - d.x) * inv_denom) + erfc_sum_term((dc - d.y) * inv_denom);
+        if (has_prev) {
+          const float2 pp = pv[e];
+          const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
+          const unsigned bx = __ballot_sync(0xffffffffu, px);
+          const unsigned by = __ballot_sync(0xffffffffu, py);
+          if (a.update == 0) {
+            // pair-major bitmap: one 64-bit word per 32 pairs, even voxels in the low half;
+            // a fire-and-forget OR, so nothing on the warp's path waits for memory
+            if (lane == 0 && (bx | by))
+              atomicOr(reinterpret_cast<unsigned long long*>(a.flags) + (pair0 + e) / 32,
+                       ((unsigned long long)by << 32) | bx);
+          } else if (bx | by) {
+            const unsigned cnt = __popc(bx) + __popc(by);
+            unsigned first = 0;
+            if (lane == 0) first = atomicAdd(a.center_count, cnt);
+            first = __shfl_sync(0xffffffffu, first, 0);
+            const unsigned lt = (1u << lane) - 1u;
+            const unsigned v0 = (unsigned)((pair0 + e) * 2);
+            unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
+            if (px) a.centers[pos++] = v0;
+            if (py) a.centers[pos] = v0 + 1;
+          }
+        }
+        a.rout[pair0 + e] = d;
+      }
+    }
+    __syncthreads();                                   // S[s], P[s], A, B free again
+    if (threadIdx.x == 0 && it + 2 < my_count) {
+      fence_async_smem();
+      issue(it + 2, s);
+    }
+  }
+  if (EPI == EPI_IONIZE) {
+    float total;
+    if (grid_sum<T>(acc, a.partials, a.counter, sred, &total) && threadIdx.x == 0) {
+      const float mean = total / ((float)N * (float)N * (float)N);
+      a.stats_out[0] = total;
+      a.stats_out[1] = mean;
+      a.stats_out[2] = a.normalize ? a.fc_mean / mean : 1.f;
+    }
+  }
+}
+
+// Real rows -> half-spectrum rows (slot 0 holds (X[0], X[N/2])), with a scale or P(k) prologue.
+template <int N, int PRO, int V>
+__global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_r2c(const __grid_constant__ OpArgs a) {
+  constexpr int M = N / 2, RL = RowTile<N, V>::RL, T = RowTile<N, V>::T, ES = RL + 1;
+  using SM = Row2Smem<N, false, V>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  float2* const S0 = reinterpret_cast<float2*>(base);
+  float2* const S1 = reinterpret_cast<float2*>(base + SM::stage);
+  float2* A = reinterpret_cast<float2*>(base + 2 * SM::stage);
+  float2* B = A + M * ES;
+  float2* tw = B + M * ES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + N);
+  __shared__ int s_abort;
+
+  const int ntiles = N * N / RL;
+  const int my_count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const uint32_t tile_bytes = RL * M * 8;
+  auto issue = [&](int it, int s) {
+    const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
+    mbar_expect_tx(&bars[s], tile_bytes);
+    bulk_load(s ? S1 : S0, a.rin + pair0, tile_bytes, &bars[s]);
+  };
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+    fence_async_smem();
+    for (int s = 0; s < 2 && s < my_count; ++s) issue(s, s);
+  }
+  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
+  float sc = a.scale, sh = 0.f;
+  if (PRO == PRO_PK) {
+    const float ave = *a.ave;
+    // g = (x / ave - 1) V / N^3  (delta_T.py:80-82), optionally times ave
+    sc = a.pk_norm / ave;
+    sh = -a.pk_norm;
+    if (a.dimensional) { sc *= ave; sh *= ave; }
+  }
+  __syncthreads();
+
+  for (int it = 0; it < my_count; ++it) {
+    const int s = it & 1;
+    const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
+    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1))) {
+      atomicOr(a.err, ES_DEV_ERR_TIMEOUT);
+      s_abort = 1;
+    }
+    __syncthreads();
+    if (s_abort) break;
+    const float2* src = s ? S1 : S0;
+    for (int e = threadIdx.x; e < RL * M; e += T) {
+      const int row = e / M, p = e % M;
+      float2 v = src[e];
+      v = PRO == PRO_PK ? make_float2(fmaf(v.x, sc, sh), fmaf(v.y, sc, sh)) : cscale(v, sc);
+      A[p * ES + row] = v;
+    }
+    __syncthreads();
+    float2* Z = fft_lines<M, false, RL, T, true, ES, 1, N>(A, B, tw);
+    // X[m] = (Z[m] + conj Z[M-m]) / 2 - i w^m (Z[m] - conj Z[M-m]) / 2
+    for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += T) {
+      const int m = q % (M / 2 + 1), l = q / (M / 2 + 1);
+      float2* out = a.cout + pair0 + (size_t)l * M;
+      if (m == 0) {
+        const float2 z0 = Z[l];
+        out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+      } else {
+        const int m2 = M - m;
+        const float2 zm = Z[m * ES + l], zc = Z[m2 * ES + l];
+        {
+          const float2 t = cmul(tw[m], make_float2(zm.x - zc.x, zm.y + zc.y));
+          out[m] = make_float2(0.5f * (zm.x + zc.x + t.y), 0.5f * (zm.y - zc.y - t.x));
+        }
+        if (m2 != m) {
+          const float2 t = cmul(tw[m2], make_float2(zc.x - zm.x, zc.y + zm.y));
+          out[m2] = make_float2(0.5f * (zc.x + zm.x + t.y), 0.5f * (zc.y - zm.y - t.x));
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && it + 2 < my_count) {
+      fence_async_smem();
+      issue(it + 2, s);
+    }
+  }
+}
+
+}  // namespace es

@@ -1,0 +1,369 @@
+// TMA-fed column passes (sm_103a): tiles of TI spectrum columns x N elements move between HBM and
+// shared memory with cp.async.bulk.tensor, two tiles in flight per CTA, completion tracked by
+// mbarriers.  Every wait is bounded; a timeout sets the plan's error word and the CTA leaves.
+#pragma once
+#include <cuda.h>
+#include "es_kernels.cuh"
+
+namespace es {
+
+constexpr unsigned ES_DEV_ERR_TIMEOUT = 1u;
+constexpr long kWaitLimit = 1L << 26;      // mbarrier polls before a wait is declared hung
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load2(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store3(const CUtensorMap* map, const void* src, int c0, int c1, int c2) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];"
+               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2)
+               : "memory");
+}
+__device__ __forceinline__ void tma_store2(const CUtensorMap* map, const void* src, int c0, int c1) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%2, %3}], [%1];"
+               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(src)), "r"(c0), "r"(c1)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// Stage 0 of a line FFT with a hook applied to every loaded element (filter, column packing).
+template <int N, bool INV, int NL, int T, int ES, int TWN, class Pre>
+__device__ __forceinline__ void stockham_stage0_pre(const float2* __restrict__ in, float2* __restrict__ out,
+                                                    const float2* __restrict__ tw, Pre pre) {
+  constexpr int R = Plan<N>::radix[0];
+  constexpr int NB = NL * (N / R);
+  for (int b = threadIdx.x; b < NB; b += T) {
+    const int l = b % NL, j = b / NL;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = pre(l, j + r * (N / R), in[l + (j + r * (N / R)) * ES]);
+    Dft<R, INV>::run(v);                      // Ns = 1: no twiddles in the first stage
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[l + (j * R + r) * ES] = v[r];
+  }
+}
+
+template <int N, bool INV, int NL, int T, int ES, int TWN, class Pre>
+__device__ __forceinline__ float2* fft_columns_pre(float2* a, float2* b, const float2* tw, Pre pre) {
+  stockham_stage0_pre<N, INV, NL, T, ES, TWN>(a, b, tw, pre);
+  __syncthreads();
+  return Stages<N, 1, INV, NL, T, true, ES, 1, TWN>::run(b, a, tw);
+}
+
+// TMA column-pass tile shapes: variant 0 = (TI columns, T threads) of the synchronous pass,
+// 1 = half as wide with half the threads (smaller shared memory, more CTAs per SM),
+// 2 = TI columns with twice the threads (more warps to hide latency).
+template <int N, int V> struct ColTile {
+  static constexpr int TI = V == 1 ? ColCfg<N>::TI / 2 : ColCfg<N>::TI;
+  static constexpr int T = V == 1 ? ColCfg<N>::T / 2 : (V == 2 ? 2 * ColCfg<N>::T : ColCfg<N>::T);
+  static constexpr int MINB = T >= 512 ? 2 : 1;       // keep two 512-thread CTAs resident
+};
+
+struct TileCoord { int plane, c; bool nyq; };
+
+template <int N, int MODE, int V>
+__device__ __forceinline__ TileCoord tile_coord(int tile) {
+  constexpr int CPR = (N / 2) / ColTile<N, V>::TI;
+  constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
+  TileCoord t;
+  const int nmain = N * CPR;
+  if (ZPASS && tile >= nmain) { t.nyq = true; t.plane = 0; t.c = tile - nmain; }
+  else { t.nyq = false; t.plane = tile / CPR; t.c = tile % CPR; }
+  return t;
+}
+
+// Tile load: z-pass boxes are (TI, 1, BOX) at (c TI, j, k0); y-pass boxes (TI, BOX, 1) at (c TI, j0, k);
+// Nyquist-plane boxes (TI, BOX) at (c TI, k0).  BOX = min(N, 256) (a TMA box side is <= 256).
+template <int N, int MODE, int V>
+__device__ __forceinline__ void issue_tile_load(const OpArgs& a, const TileCoord& t, float2* dst, uint64_t* bar) {
+  constexpr int TI = ColTile<N, V>::TI;
+  constexpr int BOX = N < 256 ? N : 256;
+  constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
+  mbar_expect_tx(bar, (uint32_t)(N * TI * 8));
+#pragma unroll
+  for (int h = 0; h < N / BOX; ++h) {
+    float2* d = dst + h * BOX * TI;
+    if (t.nyq) tma_load2(d, &a.tm_in_nyq, bar, t.c * TI, h * BOX);
+    else if (ZPASS) tma_load3(d, &a.tm_in, bar, t.c * TI, t.plane, h * BOX);
+    else tma_load3(d, &a.tm_in, bar, t.c * TI, h * BOX, t.plane);
+  }
+}
+
+template <int N, int MODE, int V>
+__device__ __forceinline__ void issue_tile_store(const OpArgs& a, const TileCoord& t, const float2* src) {
+  constexpr int TI = ColTile<N, V>::TI;
+  constexpr int BOX = N < 256 ? N : 256;
+  constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
+#pragma unroll
+  for (int h = 0; h < N / BOX; ++h) {
+    const float2* s = src + h * BOX * TI;
+    if (t.nyq) tma_store2(&a.tm_out_nyq, s, t.c * TI, h * BOX);
+    else if (ZPASS) tma_store3(&a.tm_out, s, t.c * TI, t.plane, h * BOX);
+    else tma_store3(&a.tm_out, s, t.c * TI, h * BOX, t.plane);
+  }
+  bulk_commit();
+}
+
+template <int N, int MODE, int V> struct TmaSmem {
+  static constexpr int TI = ColTile<N, V>::TI, T = ColTile<N, V>::T;
+  static constexpr int tile = N * TI * 8;
+  static constexpr int pk = (MODE == COL_Z_FWD_PK)
+      ? ((T / 32) * PK_MAX_BINS * 3 + (T / 32) * 32 * 4 + PK_MAX_BINS) * 4
+      : (MODE == COL_Z_INV_FILTER ? TI * (N / 2 + 1) * 4 : 0);    // per-tile filter weights
+  // [S0 | S1 | W | twiddles | pk bins or filter weights | 2 mbarriers] after aligning the base
+  static constexpr int bytes = 3 * tile + N * 8 + pk + 16 + 128;
+};
+
+template <int N, int MODE, int V>
+__global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma(const __grid_constant__ OpArgs a) {
+  constexpr int M = N / 2;
+  constexpr int TI = ColTile<N, V>::TI, T = ColTile<N, V>::T;
+  constexpr bool INV = (MODE == COL_Z_INV_FILTER || MODE == COL_Y_INV || MODE == COL_Z_INV);
+  constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
+  constexpr int CPR = M / TI;
+  constexpr bool RESULT_IN_W = (Plan<N>::stages % 2) == 1;
+  const int ntiles = ZPASS ? N * CPR + N / TI : N * CPR;
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // TMA destinations must be 128-byte aligned: align the base explicitly (128 bytes of slack)
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  float2* S0 = reinterpret_cast<float2*>(base);
+  float2* S1 = S0 + N * TI;
+  float2* W = S1 + N * TI;
+  float2* tw = W + N * TI;
+  float* bins = reinterpret_cast<float*>(tw + N);
+  float* wcol = bins;                         // COL_Z_INV_FILTER: W[col][|kz|], TI x (N/2 + 1)
+  float* scratch = bins + (T / 32) * PK_MAX_BINS * 3;
+  int* sthr = reinterpret_cast<int*>(scratch + (T / 32) * 32 * 4);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + 3 * TmaSmem<N, MODE, V>::tile + N * 8 + TmaSmem<N, MODE, V>::pk);
+  __shared__ int s_abort;
+
+  const int my_count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+    fence_async_smem();
+    for (int s = 0; s < 2 && s < my_count; ++s)
+      issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + s * gridDim.x), s ? S1 : S0, &bars[s]);
+  }
+  for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
+  if (MODE == COL_Z_FWD_PK) {
+    for (int i = threadIdx.x; i < (T / 32) * PK_MAX_BINS * 3; i += T) bins[i] = 0.f;
+    for (int i = threadIdx.x; i < a.nbins; i += T) sthr[i] = a.thr[i];
+  }
+  __syncthreads();
+
+  for (int it = 0; it < my_count; ++it) {
+    const int s = it & 1;
+    float2* S = s ? S1 : S0;
+    const TileCoord t = tile_coord<N, MODE, V>(blockIdx.x + it * gridDim.x);
+    if (MODE == COL_Z_INV_FILTER) {
+      // W depends on |k|^2 = kz^2 + (ky^2 + kx^2 of the column): N/2 + 1 distinct values per
+      // column.  Computed before waiting for the tile, so the arithmetic overlaps the copy.
+      const float scale = a.scale * a.inv_n3;
+      for (int q = threadIdx.x; q < TI * (M + 1); q += T) {
+        const int col = q / (M + 1), kz = q % (M + 1);
+        const int ck2 = !t.nyq ? wrap2<N>(t.plane) + (t.c * TI + col) * (t.c * TI + col)
+                               : wrap2<N>(t.c * TI + col) + M * M;
+        wcol[q] = filter_weight(kz * kz + ck2, a.dk, a.fR, a.fk2cut, a.filter, a.ref_compat) * scale;
+      }
+    }
+    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1))) {
+      atomicOr(a.err, ES_DEV_ERR_TIMEOUT);
+      s_abort = 1;
+    }
+    __syncthreads();
+    if (s_abort) break;
+
+    float2* out;
+    if (MODE == COL_Z_INV_FILTER) {
+      out = fft_columns_pre<N, INV, TI, T, TI, N>(S, W, tw, [&](int col, int k, float2 v) {
+        return cscale(v, wcol[col * (M + 1) + (k > M ? N - k : k)]);
+      });
+    } else if (MODE == COL_Y_INV) {
+      const float2* nyq = a.cin_nyq + (size_t)t.plane * N;
+      const bool pack = t.c == 0;
+      out = fft_columns_pre<N, INV, TI, T, TI, N>(S, W, tw, [&](int col, int j, float2 v) {
+        if (pack && col == 0) {                      // u = y0 + i yM (both Hermitian columns)
+          const float2 ym = nyq[j];
+          v = make_float2(v.x - ym.y, v.y + ym.x);
+        }
+        return v;
+      });
+    } else {
+      out = fft_columns_pre<N, INV, TI, T, TI, N>(S, W, tw, [](int, int, float2 v) { return v; });
+    }
+    (void)RESULT_IN_W;
+
+    if (MODE == COL_Z_FWD_PK) {
+      // Each thread runs down KR consecutive kz of one column, where |k| changes slowly, and
+      // accumulates one bin at a time; when a lane's bin changes, the warp merges the finished
+      // runs of all lanes that changed (grouped by bin, summed in lane order: deterministic).
+      constexpr int NSEG = T / TI;                          // k segments per column
+      constexpr int KR = (N + NSEG - 1) / NSEG;             // kz per segment (last may be short)
+      static_assert(NSEG * TI == T, "threads must cover whole columns");
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      float* wb = bins + warp * PK_MAX_BINS * 3;
+      float* ws = scratch + warp * 32 * 4;
+      const float inv = 1.0f / (2.0f * 9.8696044010893586f * a.volume);
+      const int col = threadIdx.x % TI, k0 = (threadIdx.x / TI) * KR;
+      int ck2;
+      float wgt;
+      if (!t.nyq) { const int kx = t.c * TI + col; ck2 = wrap2<N>(t.plane) + kx * kx; wgt = kx == 0 ? 1.f : 2.f; }
+      else { ck2 = wrap2<N>(t.c * TI + col) + M * M; wgt = 1.f; }
+      int cur = -1;
+      float ap = 0.f, ak = 0.f, an = 0.f;
+      auto flush = [&](bool mine) {
+        const int key = mine ? cur : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        ws[lane * 4 + 0] = ap; ws[lane * 4 + 1] = ak; ws[lane * 4 + 2] = an;
+        __syncwarp();
+        if (mine && lane == __ffs(peers) - 1) {
+          float p = 0.f, k = 0.f, n = 0.f;
+          unsigned m = peers;
+          while (m) {
+            const int l = __ffs(m) - 1;
+            m &= m - 1;
+            p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += ws[l * 4 + 2];
+          }
+          wb[cur] += p; wb[PK_MAX_BINS + cur] += k; wb[2 * PK_MAX_BINS + cur] += n;
+        }
+        __syncwarp();
+      };
+      for (int q = 0; q < KR; ++q) {                         // warp-uniform trip count
+        const int k = k0 + q;
+        const bool valid = k < N;
+        const int k2 = wrap2<N>(valid ? k : 0) + ck2;
+        int lo = 0, hi = a.nbins;                            // first bin with k2 <= thr[bin]
+        while (lo < hi) { const int mid = (lo + hi) >> 1; if (k2 <= sthr[mid]) hi = mid; else lo = mid + 1; }
+        const int bin = (k2 == 0 || !valid) ? a.nbins : lo;    // the mean (k = 0) is excluded
+        const bool change = bin != cur;
+        if (__any_sync(0xffffffffu, change && cur >= 0 && cur < a.nbins))
+          flush(change && cur >= 0 && cur < a.nbins);
+        if (change) { cur = bin; ap = ak = an = 0.f; }
+        if (!valid) continue;
+        const float2 g = out[k * TI + col];
+        const float km = a.dk * sqrtf((float)k2);
+        ap += wgt * km * km * km * (g.x * g.x + g.y * g.y) * inv;
+        ak += wgt * km;
+        an += wgt;
+      }
+      flush(cur >= 0 && cur < a.nbins);
+      __syncthreads();
+    } else {
+      if (MODE == COL_Y_FWD && t.c == 0) {
+        // split the packed column 0: FFT(x0) stays in column 0, FFT(xM) goes to the nyq plane
+        constexpr int Q = (N + T - 1) / T;
+        float2 av[Q], bv[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int j = threadIdx.x + q * T;
+          if (j < N) {
+            const float2 v = out[j * TI];
+            const float2 w = out[((N - j) % N) * TI];
+            av[q] = make_float2(0.5f * (v.x + w.x), 0.5f * (v.y - w.y));
+            bv[q] = make_float2(0.5f * (v.y + w.y), -0.5f * (v.x - w.x));
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int j = threadIdx.x + q * T;
+          if (j < N) {
+            out[j * TI] = av[q];
+            a.cout_nyq[(size_t)t.plane * N + j] = bv[q];
+          }
+        }
+      }
+      fence_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) issue_tile_store<N, MODE, V>(a, t, out);
+    }
+    if (threadIdx.x == 0 && it + 2 < my_count) {
+      bulk_wait_read0();                  // the store above has finished reading shared memory
+      fence_async_smem();
+      issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + (it + 2) * gridDim.x), S, &bars[s]);
+    } else if (threadIdx.x == 0) {
+      bulk_wait_read0();
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bulk_wait0();
+
+  if (MODE == COL_Z_FWD_PK) {
+    __syncthreads();
+    const int nb3 = 3 * a.nbins;
+    for (int idx = threadIdx.x; idx < nb3; idx += T) {
+      const int q = idx / a.nbins, bin = idx % a.nbins;
+      float s = 0.f;
+      for (int w = 0; w < T / 32; ++w) s += bins[w * PK_MAX_BINS * 3 + q * PK_MAX_BINS + bin];
+      a.partials[(size_t)blockIdx.x * nb3 + idx] = s;
+    }
+    __shared__ unsigned s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      float* tot = bins;
+      for (int idx = threadIdx.x; idx < nb3; idx += T) {
+        float s = 0.f;
+        for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(a.partials + (size_t)b * nb3 + idx);
+        tot[idx] = s;
+      }
+      __syncthreads();
+      for (int bin = threadIdx.x; bin < a.nbins; bin += T) {
+        const float n = tot[2 * a.nbins + bin];
+        a.pk_out[bin] = n > 0.f ? tot[bin] / n : 0.f;
+        a.pk_out[a.nbins + bin] = n > 0.f ? tot[a.nbins + bin] / n : 0.f;
+        a.pk_out[2 * a.nbins + bin] = n;
+      }
+      if (threadIdx.x == 0) *a.counter = 0u;
+    }
+  }
+}
+
+}  // namespace es

@@ -166,6 +166,28 @@ class ExcursionSetPlan:
         _lib.check("es_fft_c2r", self.lib.es_fft_c2r(self.handle, _ptr(X), _ptr(out), _stream_handle(self.device, stream)), self.lib)
         return out
 
+    # ------------------------------------------------------------------ options and health
+    def set_option(self, option: int, value: int):
+        _lib.check("es_plan_set_option", self.lib.es_plan_set_option(self.handle, int(option), int(value)), self.lib)
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int()
+        _lib.check("es_plan_get_option", self.lib.es_plan_get_option(self.handle, int(option), C.byref(v)), self.lib)
+        return int(v.value)
+
+    @property
+    def col_variant(self) -> int:
+        """Column-pass implementation: 1 TMA double-buffered tiles, 0 synchronous tiles."""
+        return self.get_option(_lib.OPT_COL_VARIANT)
+
+    @col_variant.setter
+    def col_variant(self, v: int):
+        self.set_option(_lib.OPT_COL_VARIANT, v)
+
+    def check(self, stream=None):
+        """Synchronise and raise EngineError if a kernel of this plan gave up a bounded wait."""
+        _lib.check("es_plan_check", self.lib.es_plan_check(self.handle, _stream_handle(self.device, stream)), self.lib)
+
     # ------------------------------------------------------------------ per-launch timing
     def profile_enable(self, max_launches: int):
         """Bracket each kernel this plan launches with CUDA events (0 turns it off)."""

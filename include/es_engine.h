@@ -25,6 +25,7 @@ extern "C" {
 #define ES_E_CUDA (-2)       /* a CUDA runtime call failed */
 #define ES_E_NOMEM (-3)      /* workspace allocation failed */
 #define ES_E_UNSUPPORTED (-4) /* box size without compiled kernels */
+#define ES_E_DEVICE (-5)     /* a kernel reported a timed-out wait through the plan's error word */
 
 typedef struct es_plan es_plan;
 
@@ -61,6 +62,20 @@ int es_plan_destroy(es_plan* plan);
 size_t es_plan_workspace_bytes(int n, int max_radii);
 /* Box sizes with compiled kernels, written to sizes[0..cap); returns their count. */
 int es_supported_sizes(int* sizes, int cap);
+
+/* Plan options.  ES_OPT_COL_VARIANT selects the pass implementation: 1 (default) TMA tiles
+ * double-buffered on mbarriers, 0 synchronous tile loads.  ES_OPT_COL_TILE (0..2) and
+ * ES_OPT_ROW_TILE (0..3) select the TMA passes' tile shapes; the Python autotuner times them
+ * per box size and stores the fastest.  Set options between calls, never while the plan's stream
+ * has work of the plan in flight. */
+#define ES_OPT_COL_VARIANT 1
+#define ES_OPT_COL_TILE 2
+#define ES_OPT_ROW_TILE 3
+int es_plan_set_option(es_plan* plan, int option, int value);
+int es_plan_get_option(es_plan* plan, int option, int* value);
+/* Synchronises the stream and reports ES_E_DEVICE if any kernel of the plan gave up a bounded
+ * wait since the last check (the word is cleared). */
+int es_plan_check(es_plan* plan, void* stream);
 
 /* Forward transform of the density box, once per box (the reference repeats it per radius,
  * find_HII_bubbles.py:141-144).  delta: device float32 n^3. */
@@ -131,6 +146,10 @@ int es_fft_c2r(es_plan* plan, const void* in_half, float* out, void* stream);
 int es_profile_enable(es_plan* plan, int max_launches);
 int es_profile_reset(es_plan* plan);
 int es_profile_read(es_plan* plan, float* total_ms, int* counts, int nops);
+
+/* Self-test of the erfc used for the per-radius sum of fcoll: writes it (fast) and the CUDA
+ * library's erfcf (lib) for n device floats x. */
+int es_selftest_erfc(const float* x, float* fast, float* lib, int n, void* stream);
 
 /* Message of the calling thread's last failure, copied into buf (NUL-terminated). */
 int es_last_error(char* buf, int len);

@@ -135,6 +135,71 @@ def test_sphere_painting_matches_oracle(eng, ref_compat):
     _compare_ionized(out.cpu().numpy().astype(np.float64), ref, f"sphere ref_compat={ref_compat}")
 
 
+@pytest.mark.parametrize("n,L", [(32, 48.0), (48, 72.0), (96, 144.0), (256, 300.0)])
+def test_tile_variants_agree(eng, n, L):
+    # every tile-shape candidate of the autotuner (TMA and synchronous passes) runs the same
+    # transforms; they differ only in where the compiler contracts the filter multiply into FMAs
+    at = module("autotune")
+    z = 8.0
+    d = torch.from_numpy(grf.density_box(n, L, seed=1, z=z)).cuda()
+    st = _setup(n, L, z, R_max=min(15.0, 0.2 * L))
+    c = cos.brightness_temperature_factor(z, cos.BASELINE_COSMO)
+    edges = sch.pk_edges(n, L, 20)
+    outs = {}
+    with _plan(eng, n, L) as p:
+        for cfg in at.CANDIDATES:
+            at.apply(p, cfg)
+            xh, nf = p.run(d, st)
+            dT, ave = p.delta_T(xh, d, c)
+            pk = p.power_spectrum(dT, ave, edges)
+            X = p.fft_r2c(d)
+            outs[cfg] = (xh.clone(), nf.item(), pk.clone(), X.clone())
+        p.check()
+    ref = outs[at.CANDIDATES[0]]
+    for cfg, (xh, nf, pk, X) in outs.items():
+        diff = (xh - ref[0]).abs()
+        assert (diff > PARTIAL_ATOL).float().mean().item() <= 1e-5, cfg
+        assert abs(nf - ref[1]) <= 1e-6, cfg
+        assert torch.equal(pk[2], ref[2][2]), cfg
+        nz = ref[2][2] > 0
+        assert torch.allclose(pk[0][nz], ref[2][0][nz], rtol=1e-5), cfg
+        assert ((X - ref[3]).abs().max() / ref[3].abs().max()).item() < 1e-6, cfg
+
+
+def test_sum_erfc_against_library_and_float64(eng):
+    # the per-radius fcoll sum uses Numerical Recipes' erfcc; check it against CUDA's erfcf and
+    # against float64 scipy over the arguments the engine meets (and well beyond)
+    import ctypes as C
+    from scipy.special import erfc
+    _lib = module("_lib")
+    lib = _lib.load()
+    x = torch.linspace(-6.0, 10.0, 400001, device="cuda")
+    fast, ref = torch.empty_like(x), torch.empty_like(x)
+    rc = lib.es_selftest_erfc(C.c_void_p(x.data_ptr()), C.c_void_p(fast.data_ptr()), C.c_void_p(ref.data_ptr()),
+                              x.numel(), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check("es_selftest_erfc", rc, lib)
+    xd = x.cpu().numpy().astype(np.float64)
+    exact = erfc(xd)
+    keep = exact > 1e-30
+    rel_fast = np.abs(fast.cpu().numpy()[keep] - exact[keep]) / exact[keep]
+    rel_lib = np.abs(ref.cpu().numpy()[keep] - exact[keep]) / exact[keep]
+    # the cells that carry the sum have |x| < 3 (erfc > 2e-5); beyond, a few 1e-6 do not matter
+    core = np.abs(xd[keep]) < 3.0
+    assert rel_fast[core].max() < 2e-6, rel_fast[core].max()
+    assert rel_fast.max() < 2e-5, rel_fast.max()
+    assert rel_lib.max() < 1e-6
+    # what the engine uses it for: the mean over cells, here weighted like a smoothed density
+    # field's x = (delta_c - delta_R) / denom, must agree to well below the 1e-5 flag tolerance
+    w = np.exp(-0.5 * ((xd - 1.5) / 1.0) ** 2)
+    mean_fast = np.sum(w * fast.cpu().numpy()) / np.sum(w)
+    mean_exact = np.sum(w * exact) / np.sum(w)
+    assert abs(mean_fast / mean_exact - 1) < 2e-7
+    # no bias: the mean signed error over a band of typical arguments stays tiny
+    band = (xd > -1) & (xd < 4)
+    signed = (fast.cpu().numpy()[band] - exact[band]) / exact[band]
+    assert abs(signed.mean()) < 1e-7
+
+
 def test_ionize_is_deterministic(eng):
     n, L, z = 64, 100.0, 8.0
     d = torch.from_numpy(grf.density_box(n, L, seed=0, z=z)).cuda()
