@@ -22,6 +22,7 @@ ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", 
 OPT_COL_VARIANT = 1
 OPT_COL_TILE = 2
 OPT_ROW_TILE = 3
+OPT_L2_HINTS = 4
 
 
 class EngineUnavailable(RuntimeError):

@@ -106,6 +106,8 @@ struct es_plan {
   CUtensorMap tmX_z, tmX_y, tmXn, tmT_z, tmT_y, tmTn;
   int col_variant = 1;              // passes: 1 TMA double-buffered (default), 0 synchronous
   int col_tile = 0, row_tile = 0;   // TMA tile-shape variants
+  int l2_hints = 1;                 // keep the intermediate spectrum in L2 when it fits
+  long l2_bytes = 0;                // device L2 size
   unsigned* err = nullptr;          // device error word (timed-out waits)
 };
 
@@ -516,6 +518,7 @@ int es_plan_create(int n, double box_len, int max_radii, es_plan** out) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, p->device) != cudaSuccess) return cleanup(fail(ES_E_CUDA, "cudaGetDeviceProperties failed"));
   p->sms = prop.multiProcessorCount;
+  p->l2_bytes = prop.l2CacheSize;
   p->partial_floats = partial_floats_for(p->sms, p->geo);
   Layout L = layout(n, max_radii, p->partial_floats);
   if (cudaMalloc(&p->base, L.total) != cudaSuccess) {
@@ -633,6 +636,13 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
   const size_t N3 = (size_t)p->n * p->n * p->n;
   ES_CUDA(cudaMemsetAsync(p->flags, 0, N3 / 8, s));
   const float inv_zeta = (float)(1.0 / (double)prm->zeta);
+  // The intermediate spectrum T is written by the z pass, rewritten by the y pass and read by the
+  // row pass; when it fits comfortably in L2 it is kept there (evict_last) while the input
+  // spectrum and the delta_R boxes stream (evict_first), and the row pass drops T's consumed
+  // lines so the dead data is never written back.
+  const size_t t_bytes = (size_t)p->n * p->n * (p->m + 1) * sizeof(float2);
+  const bool keep_T = p->l2_hints && (double)t_bytes <= 0.6 * (double)p->l2_bytes;
+  const int keep = keep_T ? es::ES_HINT_EVICT_LAST : es::ES_HINT_NORMAL;
   for (int r = 0; r < nr; ++r) {
     es::OpArgs a = base_args(p);
     a.cin = p->X; a.cin_nyq = p->Xnyq; a.cout = p->T; a.cout_nyq = p->Tnyq;
@@ -644,10 +654,14 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     a.ref_compat = prm->ref_compat;
     a.dk = p->dk;
     a.inv_n3 = inv_n3;
+    a.hint_in = p->l2_hints ? es::ES_HINT_EVICT_FIRST : es::ES_HINT_NORMAL;
+    a.hint_out = keep;
     set_maps(a, p->tmX_z, p->tmT_z, &p->tmXn, &p->tmTn);
     if ((rc = run_op(p, es::OP_COL_Z_INV_FILTER, a, grid_col_z(p, false), s))) return rc;
     a = base_args(p);
     a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T;
+    a.hint_in = keep;
+    a.hint_out = keep;
     set_maps(a, p->tmT_y, p->tmT_y, nullptr, nullptr);
     if ((rc = run_op(p, es::OP_COL_Y_INV, a, grid_col_y(p), s))) return rc;
     if (prm->update == 1 && r > 0) ES_CUDA(cudaMemsetAsync(p->counters + 1, 0, sizeof(unsigned), s));
@@ -668,6 +682,8 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     a.center_count = p->counters + 1;
     a.fc_mean = prm->fc_mean_ps;
     a.normalize = prm->normalize_mean;
+    a.hint_in = p->l2_hints ? es::ES_HINT_EVICT_FIRST : es::ES_HINT_NORMAL;
+    a.discard_in = p->l2_hints;
     if ((rc = run_op(p, es::OP_ROW_C2R_IONIZE, a, grid_row(p, true), s))) return rc;
     if (prm->update == 1 && r > 0) {
       slot = prof_begin(p, ES_PROF_PAINT, s);
@@ -841,6 +857,10 @@ int es_plan_set_option(es_plan* p, int option, int value) {
       if (value < 0 || value >= es::kRowTileVariants) return fail(ES_E_ARG, "es_plan_set_option: row tile variant out of range");
       p->row_tile = value;
       return ES_OK;
+    case ES_OPT_L2_HINTS:
+      if (value != 0 && value != 1) return fail(ES_E_ARG, "es_plan_set_option: L2 hints must be 0 or 1");
+      p->l2_hints = value;
+      return ES_OK;
     default:
       return fail(ES_E_ARG, "es_plan_set_option: unknown option %d", option);
   }
@@ -852,6 +872,7 @@ int es_plan_get_option(es_plan* p, int option, int* value) {
     case ES_OPT_COL_VARIANT: *value = p->col_variant; return ES_OK;
     case ES_OPT_COL_TILE: *value = p->col_tile; return ES_OK;
     case ES_OPT_ROW_TILE: *value = p->row_tile; return ES_OK;
+    case ES_OPT_L2_HINTS: *value = p->l2_hints; return ES_OK;
     default: return fail(ES_E_ARG, "es_plan_get_option: unknown option %d", option);
   }
 }

@@ -21,6 +21,8 @@ namespace es {
 enum ColMode { COL_Z_FWD = 0, COL_Y_FWD = 1, COL_Z_INV_FILTER = 2, COL_Y_INV = 3, COL_Z_FWD_PK = 4, COL_Z_INV = 5 };
 enum RowPro { PRO_SCALE = 0, PRO_PK = 1 };
 enum RowEpi { EPI_STORE = 0, EPI_IONIZE = 1 };
+// L2 policies of the TMA copies
+enum { ES_HINT_NORMAL = 0, ES_HINT_EVICT_FIRST = 1, ES_HINT_EVICT_LAST = 2 };
 
 constexpr int PK_MAX_BINS = 128;
 
@@ -30,6 +32,8 @@ struct OpArgs {
   unsigned* err;                  // device error word (bounded waits that timed out)
   int variant;                    // passes: 0 synchronous tiles, 1 TMA double-buffered
   int col_tile, row_tile;         // TMA tile-shape variants (chosen by the autotuner)
+  int hint_in, hint_out;          // L2 policies of the TMA loads / stores (ES_HINT_*)
+  int discard_in;                 // row pass: drop the consumed input lines from L2
   int grid;                       // CTAs to launch (persistent grid-stride)
   // real boxes viewed as float2 pairs of consecutive x
   const float2* rin;

@@ -33,9 +33,9 @@ template <int N, bool PREV, int V> struct Row2Smem {
   static constexpr int bytes = (PREV ? 4 : 2) * stage + 2 * work + N * 8 + 16 + 128;
 };
 
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
                : "memory");
 }
 
@@ -63,11 +63,12 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
   const int my_count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   const bool has_prev = PREV && a.has_prev;
   const uint32_t tile_bytes = RL * M * 8;
+  const uint64_t pol_in = l2_policy(a.hint_in), pol_prev = l2_policy(ES_HINT_EVICT_FIRST);
   auto issue = [&](int it, int s) {
     const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
     mbar_expect_tx(&bars[s], has_prev ? 2 * tile_bytes : tile_bytes);
-    bulk_load(s ? S1 : S0, a.cin + pair0, tile_bytes, &bars[s]);
-    if (has_prev) bulk_load(s ? P1 : P0, a.prev + pair0, tile_bytes, &bars[s]);
+    bulk_load(s ? S1 : S0, a.cin + pair0, tile_bytes, &bars[s], pol_in);
+    if (has_prev) bulk_load(s ? P1 : P0, a.prev + pair0, tile_bytes, &bars[s], pol_prev);
   };
   if (threadIdx.x == 0) {
     s_abort = 0;
@@ -117,6 +118,11 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
         }
       }
     }
+    if (a.discard_in) {
+      // the intermediate spectrum is dead once copied: drop its lines from L2 unwritten
+      const char* g = reinterpret_cast<const char*>(a.cin + pair0);
+      for (int l = threadIdx.x; l < (int)(tile_bytes / 128); l += T) l2_discard(g + 128 * l);
+    }
     __syncthreads();
     float2* Zr = fft_lines<M, true, RL, T, true, ES, 1, N>(A, B, tw);
     if (EPI == EPI_STORE) {
@@ -153,7 +159,7 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
             if (py) a.centers[pos] = v0 + 1;
           }
         }
-        a.rout[pair0 + e] = d;
+        __stcs(a.rout + pair0 + e, d);                 // streamed: read again only next radius
       }
     }
     __syncthreads();                                   // S[s], P[s], A, B free again
@@ -194,7 +200,7 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_r2
   auto issue = [&](int it, int s) {
     const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
     mbar_expect_tx(&bars[s], tile_bytes);
-    bulk_load(s ? S1 : S0, a.rin + pair0, tile_bytes, &bars[s]);
+    bulk_load(s ? S1 : S0, a.rin + pair0, tile_bytes, &bars[s], l2_policy(a.hint_in));
   };
   if (threadIdx.x == 0) {
     s_abort = 0;

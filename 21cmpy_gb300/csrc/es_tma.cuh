@@ -40,27 +40,44 @@ __device__ __forceinline__ void fence_async_smem() {
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+// L2 eviction-priority policies for the copies (ES_HINT_*): the intermediate spectrum is kept
+// (evict_last) while streamed inputs and outputs go first.
+__device__ __forceinline__ uint64_t l2_policy(int hint) {
+  uint64_t pol;
+  if (hint == ES_HINT_EVICT_LAST)
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  else if (hint == ES_HINT_EVICT_FIRST)
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  else
+    asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                          uint64_t pol) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, %3, %4}], [%5], %6;"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar)), "l"(pol)
       : "memory");
 }
-__device__ __forceinline__ void tma_load2(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+__device__ __forceinline__ void tma_load2(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, uint64_t pol) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, %3}], [%4], %5;"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar)), "l"(pol)
       : "memory");
 }
-__device__ __forceinline__ void tma_store3(const CUtensorMap* map, const void* src, int c0, int c1, int c2) {
-  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];"
-               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2)
+__device__ __forceinline__ void tma_store3(const CUtensorMap* map, const void* src, int c0, int c1, int c2, uint64_t pol) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group.L2::cache_hint [%0, {%2, %3, %4}], [%1], %5;"
+               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2), "l"(pol)
                : "memory");
 }
-__device__ __forceinline__ void tma_store2(const CUtensorMap* map, const void* src, int c0, int c1) {
-  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%2, %3}], [%1];"
-               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(src)), "r"(c0), "r"(c1)
+__device__ __forceinline__ void tma_store2(const CUtensorMap* map, const void* src, int c0, int c1, uint64_t pol) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group.L2::cache_hint [%0, {%2, %3}], [%1], %4;"
+               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(src)), "r"(c0), "r"(c1), "l"(pol)
                : "memory");
+}
+// drop a dead 128-byte line from L2 without writing it back
+__device__ __forceinline__ void l2_discard(const void* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
@@ -120,12 +137,13 @@ __device__ __forceinline__ void issue_tile_load(const OpArgs& a, const TileCoord
   constexpr int BOX = N < 256 ? N : 256;
   constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
   mbar_expect_tx(bar, (uint32_t)(N * TI * 8));
+  const uint64_t pol = l2_policy(a.hint_in);
 #pragma unroll
   for (int h = 0; h < N / BOX; ++h) {
     float2* d = dst + h * BOX * TI;
-    if (t.nyq) tma_load2(d, &a.tm_in_nyq, bar, t.c * TI, h * BOX);
-    else if (ZPASS) tma_load3(d, &a.tm_in, bar, t.c * TI, t.plane, h * BOX);
-    else tma_load3(d, &a.tm_in, bar, t.c * TI, h * BOX, t.plane);
+    if (t.nyq) tma_load2(d, &a.tm_in_nyq, bar, t.c * TI, h * BOX, pol);
+    else if (ZPASS) tma_load3(d, &a.tm_in, bar, t.c * TI, t.plane, h * BOX, pol);
+    else tma_load3(d, &a.tm_in, bar, t.c * TI, h * BOX, t.plane, pol);
   }
 }
 
@@ -134,12 +152,13 @@ __device__ __forceinline__ void issue_tile_store(const OpArgs& a, const TileCoor
   constexpr int TI = ColTile<N, V>::TI;
   constexpr int BOX = N < 256 ? N : 256;
   constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
+  const uint64_t pol = l2_policy(a.hint_out);
 #pragma unroll
   for (int h = 0; h < N / BOX; ++h) {
     const float2* s = src + h * BOX * TI;
-    if (t.nyq) tma_store2(&a.tm_out_nyq, s, t.c * TI, h * BOX);
-    else if (ZPASS) tma_store3(&a.tm_out, s, t.c * TI, t.plane, h * BOX);
-    else tma_store3(&a.tm_out, s, t.c * TI, h * BOX, t.plane);
+    if (t.nyq) tma_store2(&a.tm_out_nyq, s, t.c * TI, h * BOX, pol);
+    else if (ZPASS) tma_store3(&a.tm_out, s, t.c * TI, t.plane, h * BOX, pol);
+    else tma_store3(&a.tm_out, s, t.c * TI, h * BOX, t.plane, pol);
   }
   bulk_commit();
 }

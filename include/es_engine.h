@@ -71,6 +71,9 @@ int es_supported_sizes(int* sizes, int cap);
 #define ES_OPT_COL_VARIANT 1
 #define ES_OPT_COL_TILE 2
 #define ES_OPT_ROW_TILE 3
+/* ES_OPT_L2_HINTS (default 1): keep the intermediate spectrum in L2 between the passes of a
+ * radius when it fits (cache-policy hints on the TMA copies, consumed lines discarded). */
+#define ES_OPT_L2_HINTS 4
 int es_plan_set_option(es_plan* plan, int option, int value);
 int es_plan_get_option(es_plan* plan, int option, int* value);
 /* Synchronises the stream and reports ES_E_DEVICE if any kernel of the plan gave up a bounded
