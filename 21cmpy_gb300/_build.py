@@ -56,8 +56,9 @@ def build(force: bool = False, jobs: int | None = None) -> Path:
     jobs = jobs or min(len(SIZES) + 1, os.cpu_count() or 4)
     units = [([cc, *ARCH, *FLAGS, f"-DES_N={n}", "-c", str(CSRC / "es_inst.cu"), "-o",
                str(BUILD / f"es_inst_{n}.o")], BUILD / f"es_inst_{n}.o") for n in SIZES]
-    units.append(([cc, *ARCH, *FLAGS, "-c", str(CSRC / "es_engine.cu"), "-o", str(BUILD / "es_engine.o")],
-                  BUILD / "es_engine.o"))
+    for unit in ("es_engine", "es_batch"):
+        units.append(([cc, *ARCH, *FLAGS, "-c", str(CSRC / f"{unit}.cu"), "-o", str(BUILD / f"{unit}.o")],
+                      BUILD / f"{unit}.o"))
     with cf.ThreadPoolExecutor(jobs) as ex:
         list(ex.map(lambda u: _run(u[0]), units))
     tmp = LIB.with_suffix(".so.tmp")

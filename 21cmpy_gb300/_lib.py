@@ -50,6 +50,11 @@ class es_ionize_params(C.Structure):
     ]
 
 
+class es_batch_box(C.Structure):
+    _fields_ = [("n", C.c_int), ("box_len", C.c_double), ("delta", C.c_void_p), ("out", C.c_void_p),
+                ("nf", C.c_void_p), ("params", es_ionize_params)]
+
+
 _PROTOS = {
     "es_plan_create": (C.c_int, [C.c_int, C.c_double, C.c_int, C.POINTER(C.c_void_p)]),
     "es_plan_destroy": (C.c_int, [C.c_void_p]),
@@ -70,6 +75,14 @@ _PROTOS = {
     "es_profile_reset": (C.c_int, [C.c_void_p]),
     "es_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int), C.c_int]),
     "es_selftest_erfc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "es_batch_create": (C.c_int, [C.POINTER(es_batch_box), C.c_int, C.POINTER(C.c_void_p)]),
+    "es_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "es_batch_check": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "es_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint),
+                                C.POINTER(C.c_int)]),
+    "es_batch_destroy": (C.c_int, [C.c_void_p]),
+    "es_batch_debug_stall": (C.c_int, [C.c_void_p, C.c_int, C.c_long]),
+    "es_batch_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_version": (C.c_int, []),
 }
@@ -113,4 +126,9 @@ def last_error(lib=None) -> str:
 
 def check(fn: str, code: int, lib=None):
     if code != ES_OK:
+        if fn.startswith("es_batch"):
+            lib = lib or load()
+            buf = C.create_string_buffer(1024)
+            lib.es_batch_last_error(buf, len(buf))
+            raise EngineError(fn, code, buf.value.decode(errors="replace"))
         raise EngineError(fn, code, last_error(lib))

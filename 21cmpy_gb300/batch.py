@@ -1,0 +1,116 @@
+"""Batched form of the engine: many boxes of uneven HII_DIM and parameters in one persistent
+launch, replayed from a captured CUDA graph (no counterpart in the reference, which runs one box
+per ``conv_bubbles`` call).
+
+Each box is a (device density, :class:`~.schedule.IonizeSetup`) pair; outputs are x_HI boxes and
+the mean x_HI of every box.  The persistent kernel walks a work queue of (box, pass, tile) items
+interleaved across boxes, so small boxes keep the whole GPU busy.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .schedule import IonizeSetup
+
+
+def _params(st: IonizeSetup, output: int):
+    rad = (_lib.es_radius * st.n_radii)()
+    for i, s in enumerate(st.steps):
+        rad[i].R = float(s.R)
+        rad[i].denom = float(s.denom)
+    prm = _lib.es_ionize_params(
+        n_radii=st.n_radii, radii=rad, delta_c=float(st.deltac32), fc_mean_ps=float(st.fc_mean_ps),
+        zeta=float(np.float32(st.zeta)), growth_scale=float(st.growth_scale),
+        normalize_mean=int(st.normalize_mean), filter_type=int(st.filter_type), update=int(st.update),
+        ref_compat=int(st.ref_compat), output=output)
+    return prm, rad
+
+
+class BatchedExcursionSet:
+    """x_HI of many boxes in one persistent launch (``es_batch_*``)."""
+
+    def __init__(self, boxes, output: str = "xH", use_graph: bool = True, device=None):
+        if not torch.cuda.is_available():
+            raise _lib.EngineUnavailable("the batched engine needs a CUDA device")
+        self.lib = _lib.load()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.use_graph = bool(use_graph)
+        self.inputs, self.setups = [], []
+        for d, st in boxes:
+            if not isinstance(d, torch.Tensor) or d.device != self.device or d.dtype != torch.float32:
+                raise ValueError("densities must be float32 tensors on the batch's device")
+            n = st.n
+            if tuple(d.shape) != (n, n, n) or not d.is_contiguous():
+                raise ValueError(f"density of a {n}^3 box must be a contiguous ({n}, {n}, {n}) tensor")
+            if st.update != 0:
+                raise ValueError("the batched engine supports centre-pixel updates only")
+            self.inputs.append(d)
+            self.setups.append(st)
+        cnt = len(self.setups)
+        if cnt == 0:
+            raise ValueError("empty batch")
+        self.out = [torch.empty_like(d) for d in self.inputs]
+        self.nf = torch.zeros(cnt, dtype=torch.float32, device=self.device)
+        arr = (_lib.es_batch_box * cnt)()
+        keep = []
+        for i, (d, st) in enumerate(zip(self.inputs, self.setups)):
+            prm, rad = _params(st, 0 if output == "xH" else 1)
+            keep.append(rad)
+            arr[i].n = st.n
+            arr[i].box_len = st.box_len
+            arr[i].delta = C.c_void_p(d.data_ptr())
+            arr[i].out = C.c_void_p(self.out[i].data_ptr())
+            arr[i].nf = C.c_void_p(self.nf.data_ptr() + 4 * i)
+            arr[i].params = prm
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            rc = self.lib.es_batch_create(arr, cnt, C.byref(h))
+        _lib.check("es_batch_create", rc, self.lib)
+        self._h = h
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("batch is closed")
+        return self._h
+
+    def run(self, stream=None):
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.device(self.device):
+            rc = self.lib.es_batch_run(self.handle, int(self.use_graph), C.c_void_p(s.cuda_stream))
+        _lib.check("es_batch_run", rc, self.lib)
+        return self.out, self.nf
+
+    def check(self, stream=None):
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check("es_batch_check", self.lib.es_batch_check(self.handle, C.c_void_p(s.cuda_stream)), self.lib)
+
+    def info(self) -> dict:
+        g, p, sm = C.c_int(), C.c_int(), C.c_int()
+        t = C.c_uint()
+        _lib.check("es_batch_info", self.lib.es_batch_info(self.handle, C.byref(g), C.byref(p), C.byref(t), C.byref(sm)), self.lib)
+        return {"grid": g.value, "passes": p.value, "tiles": t.value, "smem": sm.value}
+
+    def voxel_radius_updates(self) -> int:
+        return sum(st.n ** 3 * st.n_radii for st in self.setups)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            self.lib.es_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -150,6 +150,35 @@ int es_profile_enable(es_plan* plan, int max_launches);
 int es_profile_reset(es_plan* plan);
 int es_profile_read(es_plan* plan, float* total_ms, int* counts, int nops);
 
+/* Batched form (no counterpart in the reference, whose boxes run one at a time): many boxes of
+ * uneven HII_DIM (32..256), each with its own parameters, run in ONE persistent launch.  The
+ * host lists every box's passes (forward transform, three passes per radius, final step) level by
+ * level, interleaving boxes; CTAs take tiles from a global ticket counter in that order and start
+ * a pass once the box's previous pass has finished (bounded waits; a timeout aborts the launch and
+ * es_batch_check reports ES_E_DEVICE).  Centre-pixel updates only.  delta / out / nf are device
+ * buffers owned by the caller; es_batch_create copies the parameters and allocates the
+ * workspace of every box.  es_batch_run(use_graph = 1) captures the clear + launch into a CUDA
+ * graph on its first call and replays it afterwards. */
+typedef struct es_batch es_batch;
+typedef struct es_batch_box {
+  int n;                      /* HII_DIM */
+  double box_len;             /* BOX_LEN [Mpc] */
+  const float* delta;         /* device float32 n^3 density */
+  float* out;                 /* device float32 n^3 output (x_HI or ionised fraction) */
+  float* nf;                  /* device float: mean x_HI */
+  es_ionize_params params;    /* as for es_ionize (update must be 0) */
+} es_batch_box;
+int es_batch_create(const es_batch_box* boxes, int count, es_batch** batch);
+int es_batch_run(es_batch* batch, int use_graph, void* stream);
+int es_batch_check(es_batch* batch, void* stream);
+int es_batch_info(const es_batch* batch, int* grid, int* passes, unsigned* tiles, int* smem);
+int es_batch_destroy(es_batch* batch);
+/* Failure-detection test hook: pass `pass` waits for one tile more than its dependency
+ * completes and every wait gives up after spin_limit polls of ~100 ns.  The launch then aborts
+ * cleanly and es_batch_check reports ES_E_DEVICE; the device stays usable. */
+int es_batch_debug_stall(es_batch* batch, int pass, long spin_limit);
+int es_batch_last_error(char* buf, int len);
+
 /* Self-test of the erfc used for the per-radius sum of fcoll: writes it (fast) and the CUDA
  * library's erfcf (lib) for n device floats x. */
 int es_selftest_erfc(const float* x, float* fast, float* lib, int n, void* stream);
