@@ -114,3 +114,37 @@ class BatchedExcursionSet:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def boxes_from_specs(specs, device=None, cosmo=None, table=None):
+    """(device density, IonizeSetup) pairs for BoxSpec entries (seeded GRF at each box's z)."""
+    from .cosmology import BASELINE_COSMO
+    from .grf import density_box
+    from .schedule import ionize_setup
+    cosmo = cosmo or BASELINE_COSMO
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    out = []
+    for s in specs:
+        d = torch.from_numpy(density_box(s.n, s.box_len, s.seed, s.z, cosmo)).to(dev)
+        st = ionize_setup(s.n, s.box_len, s.z, zeta=s.zeta, t_vir_min=s.t_vir_min, R_max=s.R_max,
+                          cosmo=cosmo)
+        out.append((d, st))
+    return out
+
+
+def shard(costs, world: int):
+    """Longest-processing-time split of work items (cost per item) over `world` ranks.
+
+    Returns one list of item indices per rank; every item appears exactly once.  Boxes are
+    independent, so ranks need no collective on the data path.
+    """
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    loads = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (loads[k], k))
+        parts[r].append(i)
+        loads[r] += costs[i]
+    return [sorted(p) for p in parts]
