@@ -83,6 +83,12 @@ _PROTOS = {
     "es_batch_destroy": (C.c_int, [C.c_void_p]),
     "es_batch_debug_stall": (C.c_int, [C.c_void_p, C.c_int, C.c_long]),
     "es_batch_last_error": (C.c_int, [C.c_char_p, C.c_int]),
+    "sg_conv3d_fwd": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p]),
+    "sg_conv3d_wgrad": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_size_t, C.c_void_p]),
+    "sg_conv3d_wgrad_workspace": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
+    "sg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_version": (C.c_int, []),
 }
@@ -126,6 +132,11 @@ def last_error(lib=None) -> str:
 
 def check(fn: str, code: int, lib=None):
     if code != ES_OK:
+        if fn.startswith("sg_"):
+            lib = lib or load()
+            buf = C.create_string_buffer(1024)
+            lib.sg_last_error(buf, len(buf))
+            raise EngineError(fn, code, buf.value.decode(errors="replace"))
         if fn.startswith("es_batch"):
             lib = lib or load()
             buf = C.create_string_buffer(1024)

@@ -1,0 +1,341 @@
+// Learned-surrogate kernels: 3x3x3 circular convolutions of channels-last BF16 boxes as implicit
+// GEMMs on the tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulation).
+//
+// Layout: activations [z][y][x][C] bf16 (C contiguous); weights [27][COUT][CIN] bf16 with tap
+// index t = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1).  A CTA computes one output row (z, y): it
+// stages the nine input rows (z + dz, y + dy) and every weight in shared memory; warp w owns
+// voxels [16 w, 16 w + 16) of the row and all COUT channels.  For each tap and 16-channel step
+// the A fragment (16 voxels x 16 channels) comes from ldmatrix with one row address per voxel,
+// which also applies the circular wrap in x.
+//
+// Backward: dgrad is the same kernel on dZ with weights W'[t][ci][co] = W[26 - t][co][ci] and the
+// ReLU mask of the layer input; wgrad is, per (dz, dy) pair, a GEMM dZ^T (COUT x voxels) times the
+// shifted input (voxels x CIN) accumulated over the rows a CTA owns, with per-CTA partials summed
+// in a fixed order.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "es_engine.h"
+
+namespace sg {
+
+constexpr int WARPS = 8, THREADS = 256, MAXN = 128;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t addr, uint32_t& r0, uint32_t& r1) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0, %1}, [%2];" : "=r"(r0), "=r"(r1) : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
+}
+__device__ __forceinline__ void ldsm_x2_t(uint32_t addr, uint32_t& r0, uint32_t& r1) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0, %1}, [%2];" : "=r"(r0), "=r"(r1) : "r"(addr));
+}
+__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+enum Mode { FWD_RELU = 0, FWD_SIGMOID = 1, DGRAD_MASK = 2 };
+
+// copy n16 16-byte chunks global -> shared (plain vector loads)
+__device__ __forceinline__ void copy16(void* dst, const void* src, int chunks) {
+  const uint4* s = reinterpret_cast<const uint4*>(src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int i = threadIdx.x; i < chunks; i += THREADS) d[i] = __ldg(s + i);
+}
+
+template <int CIN, int COUT, int MODE>
+__global__ void __launch_bounds__(THREADS) conv_fwd_kernel(int n, const __nv_bfloat16* __restrict__ in,
+                                                           const __nv_bfloat16* __restrict__ w,
+                                                           const float* __restrict__ bias, void* out,
+                                                           const __nv_bfloat16* __restrict__ mask) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem);             // [27][COUT][CIN]
+  __nv_bfloat16* sx = sw + 27 * COUT * CIN;                                 // [9][n][CIN]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, tig = lane & 3;
+  copy16(sw, w, 27 * COUT * CIN * 2 / 16);
+  float b[COUT / 8][2];
+#pragma unroll
+  for (int j = 0; j < COUT / 8; ++j) {
+    b[j][0] = bias ? bias[8 * j + 2 * tig] : 0.f;
+    b[j][1] = bias ? bias[8 * j + 2 * tig + 1] : 0.f;
+  }
+  const int rows = n * n;
+  const size_t row_elems = (size_t)n * CIN;
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int z = row / n, y = row % n;
+    __syncthreads();                                      // previous row's reads of sx are done
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+      const int zz = (z + r / 3 - 1 + n) % n, yy = (y + r % 3 - 1 + n) % n;
+      copy16(sx + r * row_elems, in + ((size_t)zz * n + yy) * row_elems, (int)(row_elems * 2 / 16));
+    }
+    __syncthreads();
+    if (16 * warp >= n) continue;
+    float acc[COUT / 8][4];
+#pragma unroll
+    for (int j = 0; j < COUT / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const int vrow = 16 * warp + (lane & 15);             // this lane's A row (voxel)
+    const int khalf = (lane >> 4) * 8;
+#pragma unroll 1
+    for (int t = 0; t < 27; ++t) {
+      const int r = t / 3, dx = t % 3 - 1;
+      const int xi = (vrow + dx + n) % n;
+      const __nv_bfloat16* arow = sx + r * row_elems + (size_t)xi * CIN + khalf;
+      const __nv_bfloat16* wt = sw + t * COUT * CIN;
+#pragma unroll
+      for (int k0 = 0; k0 < CIN; k0 += 16) {
+        uint32_t a0, a1, a2, a3;
+        ldsm_x4(smem_addr(arow + k0), a0, a1, a2, a3);
+#pragma unroll
+        for (int j = 0; j < COUT / 8; ++j) {
+          uint32_t b0, b1;
+          // rows co = 8 j + (lane & 7); lanes 8..15 give the k + 8 half
+          ldsm_x2(smem_addr(wt + (8 * j + (lane & 7)) * CIN + k0 + ((lane >> 3) & 1) * 8), b0, b1);
+          mma_bf16(acc[j], a0, a1, a2, a3, b0, b1);
+        }
+      }
+    }
+    // epilogue: lane holds voxels (16 w + g) and (16 w + g + 8), channels 8 j + 2 tig + {0, 1}
+    const size_t obase = (size_t)row * n;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int x = 16 * warp + g + 8 * h;
+      const size_t v = obase + x;
+      if (MODE == FWD_SIGMOID) {
+        if (tig == 0) {
+          const float zv = acc[0][2 * h] + b[0][0];
+          reinterpret_cast<float*>(out)[v] = 1.0f / (1.0f + __expf(-zv));
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < COUT / 8; ++j) {
+          float v0 = acc[j][2 * h] + b[j][0], v1 = acc[j][2 * h + 1] + b[j][1];
+          const int ch = 8 * j + 2 * tig;
+          if (MODE == FWD_RELU) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          } else {                                        // DGRAD_MASK: ReLU of the layer input
+            const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162*>(mask + v * COUT + ch);
+            if (!(__bfloat162float(m.x) > 0.f)) v0 = 0.f;
+            if (!(__bfloat162float(m.y) > 0.f)) v1 = 0.f;
+          }
+          *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(out) + v * COUT + ch) =
+              __floats2bfloat162_rn(v0, v1);
+        }
+      }
+    }
+  }
+}
+
+// wgrad: CTA (pair p = (dz, dy) index 0..8, chunk of rows).  For its pair's three taps it
+// accumulates dW^T[tap] = X_shift^T (CIN x voxels) . dZ (voxels x COUT) over its rows: warp
+// u < 3 * (CIN / 16) owns tap dx = u / (CIN / 16) - 1 and input-channel tile u % (CIN / 16).  In the
+// CTAs of pair 4 (dz = dy = 0) the last warp also sums dZ over voxels for the bias gradient.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(THREADS) conv_wgrad_kernel(int n, const __nv_bfloat16* __restrict__ x,
+                                                             const __nv_bfloat16* __restrict__ dz,
+                                                             float* __restrict__ partials, int chunks) {
+  constexpr int MT = CIN / 16, UNITS = 3 * MT;
+  static_assert(UNITS < WARPS, "one warp must stay free for the bias gradient");
+  extern __shared__ __align__(128) unsigned char smem[];
+  __nv_bfloat16* sdz = reinterpret_cast<__nv_bfloat16*>(smem);             // [n][COUT]
+  __nv_bfloat16* sx = sdz + MAXN * COUT;                                    // [n][CIN]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, tig = lane & 3;
+  const int pair = blockIdx.x % 9, chunk = blockIdx.x / 9;
+  const int pdz = pair / 3 - 1, pdy = pair % 3 - 1;
+  const int rows = n * n;
+  const int r0 = (int)((long)rows * chunk / chunks), r1 = (int)((long)rows * (chunk + 1) / chunks);
+  float acc[COUT / 8][4];
+#pragma unroll
+  for (int j = 0; j < COUT / 8; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  float bacc = 0.f;
+  const int u = warp, dx = u / MT - 1, mt = u % MT;
+  for (int row = r0; row < r1; ++row) {
+    const int z = row / n, y = row % n;
+    const int zz = (z + pdz + n) % n, yy = (y + pdy + n) % n;
+    __syncthreads();
+    copy16(sdz, dz + (size_t)row * n * COUT, n * COUT * 2 / 16);
+    copy16(sx, x + ((size_t)zz * n + yy) * n * CIN, n * CIN * 2 / 16);
+    __syncthreads();
+    if (u < UNITS) {
+      for (int k0 = 0; k0 < n; k0 += 16) {
+        // A (ci x voxels) = transposed stored [voxel][ci] rows, shifted by dx with wrap:
+        // matrix q = lane / 8 covers ci + (q & 1) * 8 and voxels + (q >> 1) * 8
+        const int q = lane >> 3;
+        const int xs = (k0 + (q >> 1) * 8 + (lane & 7) + dx + n) % n;
+        uint32_t a0, a1, a2, a3;
+        ldsm_x4_t(smem_addr(sx + xs * CIN + 16 * mt + (q & 1) * 8), a0, a1, a2, a3);
+#pragma unroll
+        for (int j = 0; j < COUT / 8; ++j) {
+          // B (voxels x co) = stored [voxel][co], transposed delivery; lanes 0-15 give the rows
+          const int vv = k0 + (lane & 15);
+          uint32_t b0, b1;
+          ldsm_x2_t(smem_addr(sdz + vv * COUT + 8 * j), b0, b1);
+          mma_bf16(acc[j], a0, a1, a2, a3, b0, b1);
+        }
+      }
+    } else if (pair == 4 && warp == WARPS - 1) {
+      for (int c = lane; c < COUT; c += 32)
+        for (int v = 0; v < n; ++v) bacc += __bfloat162float(sdz[v * COUT + c]);
+    }
+  }
+  // partials: [cta][27][COUT][CIN] then [cta][COUT] (bias, meaningful in pair-4 CTAs)
+  float* part = partials + (size_t)blockIdx.x * (27 * COUT * CIN + COUT);
+  if (u < UNITS) {
+    float* dst = part + (size_t)(pair * 3 + dx + 1) * COUT * CIN;
+    const int ci = 16 * mt + g;
+#pragma unroll
+    for (int j = 0; j < COUT / 8; ++j) {
+      const int co = 8 * j + 2 * tig;
+      dst[co * CIN + ci] = acc[j][0];
+      dst[(co + 1) * CIN + ci] = acc[j][1];
+      dst[co * CIN + ci + 8] = acc[j][2];
+      dst[(co + 1) * CIN + ci + 8] = acc[j][3];
+    }
+  }
+  if (warp == WARPS - 1)
+    for (int c = lane; c < COUT; c += 32) part[27 * COUT * CIN + c] = pair == 4 ? bacc : 0.f;
+}
+
+// dW[27][COUT][CIN] and db[COUT]: sums of the per-CTA partials in a fixed order.  A pair's taps
+// come only from its own CTAs, so each element sums the partials of the CTAs of its pair.
+__global__ void wgrad_reduce_kernel(const float* __restrict__ partials, int ctas, int cout, int cin,
+                                    float* __restrict__ dw, float* __restrict__ db) {
+  const int per = 27 * cout * cin + cout;
+  const int chunks = ctas / 9;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < per; i += gridDim.x * blockDim.x) {
+    int pair;
+    if (i < 27 * cout * cin) pair = (i / (cout * cin)) / 3;
+    else pair = 4;
+    float s = 0.f;
+    for (int c = 0; c < chunks; ++c) s += partials[(size_t)(c * 9 + pair) * per + i];
+    if (i < 27 * cout * cin) dw[i] = s; else db[i - 27 * cout * cin] = s;
+  }
+}
+
+}  // namespace sg
+
+namespace {
+thread_local std::string g_sg_error;
+int sgfail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_sg_error = buf;
+  return code;
+}
+
+template <int CIN, int COUT, int MODE>
+int launch_fwd(int n, const void* in, const void* w, const float* bias, void* out, const void* mask, cudaStream_t s) {
+  const int smem = 27 * COUT * CIN * 2 + 9 * n * CIN * 2;
+  static unsigned configured = 0u;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto kern = sg::conv_fwd_kernel<CIN, COUT, MODE>;
+  if (!(configured & (1u << (dev & 31)))) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 27 * COUT * CIN * 2 + 9 * sg::MAXN * CIN * 2) != cudaSuccess)
+      return sgfail(ES_E_CUDA, "sg_conv3d_fwd: shared memory opt-in failed");
+    configured |= 1u << (dev & 31);
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int rows = n * n;
+  const int grid = rows < sms * 2 ? rows : sms * 2;
+  kern<<<grid, sg::THREADS, smem, s>>>(n, (const __nv_bfloat16*)in, (const __nv_bfloat16*)w, bias, out,
+                                       (const __nv_bfloat16*)mask);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return sgfail(ES_E_CUDA, "sg_conv3d_fwd launch: %s", cudaGetErrorString(e));
+  return ES_OK;
+}
+
+template <int CIN, int COUT>
+int launch_wgrad(int n, const void* x, const void* dz, float* dw, float* db, float* ws, size_t ws_bytes, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int chunks = (sms * 2 + 8) / 9;
+  if (chunks > n * n) chunks = n * n;
+  const int ctas = 9 * chunks;
+  const size_t need = (size_t)ctas * (27 * COUT * CIN + COUT) * sizeof(float);
+  if (!ws || ws_bytes < need) return sgfail(ES_E_ARG, "sg_conv3d_wgrad: workspace needs %zu bytes", need);
+  const int smem = (sg::MAXN * COUT + sg::MAXN * CIN) * 2;
+  sg::conv_wgrad_kernel<CIN, COUT><<<ctas, sg::THREADS, smem, s>>>(n, (const __nv_bfloat16*)x,
+                                                                   (const __nv_bfloat16*)dz, ws, chunks);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return sgfail(ES_E_CUDA, "sg_conv3d_wgrad launch: %s", cudaGetErrorString(e));
+  sg::wgrad_reduce_kernel<<<64, 256, 0, s>>>(ws, ctas, COUT, CIN, dw, db);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return sgfail(ES_E_CUDA, "sg_conv3d_wgrad reduce: %s", cudaGetErrorString(e));
+  return ES_OK;
+}
+
+bool shape_ok(int n) { return n >= 16 && n <= sg::MAXN && n % 16 == 0; }
+}  // namespace
+
+extern "C" {
+
+int sg_conv3d_fwd(int n, int cin, int cout, int mode, const void* in, const void* w, const float* bias, void* out,
+                  const void* mask, void* stream) {
+  if (!shape_ok(n)) return sgfail(ES_E_ARG, "sg_conv3d_fwd: n=%d must be a multiple of 16 in [16, %d]", n, sg::MAXN);
+  if (!in || !w || !out || (mode == sg::DGRAD_MASK && !mask)) return sgfail(ES_E_ARG, "sg_conv3d_fwd: NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (mode == sg::FWD_RELU) {
+    if (cin == 16 && cout == 32) return launch_fwd<16, 32, sg::FWD_RELU>(n, in, w, bias, out, mask, s);
+    if (cin == 32 && cout == 32) return launch_fwd<32, 32, sg::FWD_RELU>(n, in, w, bias, out, mask, s);
+  } else if (mode == sg::FWD_SIGMOID) {
+    if (cin == 32 && cout == 16) return launch_fwd<32, 16, sg::FWD_SIGMOID>(n, in, w, bias, out, mask, s);
+  } else if (mode == sg::DGRAD_MASK) {
+    if (cin == 32 && cout == 32) return launch_fwd<32, 32, sg::DGRAD_MASK>(n, in, w, bias, out, mask, s);
+    if (cin == 16 && cout == 32) return launch_fwd<16, 32, sg::DGRAD_MASK>(n, in, w, bias, out, mask, s);
+  }
+  return sgfail(ES_E_UNSUPPORTED, "sg_conv3d_fwd: (cin=%d, cout=%d, mode=%d) not compiled", cin, cout, mode);
+}
+
+int sg_conv3d_wgrad(int n, int cin, int cout, const void* x, const void* dz, float* dw, float* db, float* ws,
+                    size_t ws_bytes, void* stream) {
+  if (!shape_ok(n)) return sgfail(ES_E_ARG, "sg_conv3d_wgrad: n=%d must be a multiple of 16 in [16, %d]", n, sg::MAXN);
+  if (!x || !dz || !dw || !db) return sgfail(ES_E_ARG, "sg_conv3d_wgrad: NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cin == 16 && cout == 32) return launch_wgrad<16, 32>(n, x, dz, dw, db, ws, ws_bytes, s);
+  if (cin == 32 && cout == 32) return launch_wgrad<32, 32>(n, x, dz, dw, db, ws, ws_bytes, s);
+  if (cin == 32 && cout == 16) return launch_wgrad<32, 16>(n, x, dz, dw, db, ws, ws_bytes, s);
+  return sgfail(ES_E_UNSUPPORTED, "sg_conv3d_wgrad: (cin=%d, cout=%d) not compiled", cin, cout);
+}
+
+size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int chunks = (sms * 2 + 8) / 9;
+  if (chunks > n * n) chunks = n * n;
+  return (size_t)9 * chunks * (27 * cout * cin + cout) * sizeof(float);
+}
+
+int sg_last_error(char* buf, int len) {
+  if (!buf || len <= 0) return ES_E_ARG;
+  std::snprintf(buf, (size_t)len, "%s", g_sg_error.c_str());
+  return ES_OK;
+}
+
+}  // extern "C"

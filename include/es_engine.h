@@ -179,6 +179,23 @@ int es_batch_destroy(es_batch* batch);
 int es_batch_debug_stall(es_batch* batch, int pass, long spin_limit);
 int es_batch_last_error(char* buf, int len);
 
+/* Learned surrogate (no counterpart in the reference): 3x3x3 circular convolutions of
+ * channels-last BF16 boxes on the tensor cores, FP32 accumulation.  Activations [z][y][x][C] bf16,
+ * weights [27][cout][cin] bf16 with tap (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1), bias float[cout].
+ * mode 0: out = ReLU(conv + bias) bf16; mode 1: out = sigmoid(conv + bias) of channel 0 as float
+ * [n^3] (cout = 16, channels 1..15 zero weights); mode 2 (input gradient): out = conv(dZ, W') * 1[mask > 0]
+ * bf16, with W'[t][ci][co] = W[26 - t][co][ci] and mask the layer's input activations.
+ * n: multiple of 16 up to 128.  Compiled (cin, cout): mode 0 (16, 32), (32, 32); mode 1 (32, 16);
+ * mode 2 (32, 32), (16, 32); wgrad (16, 32), (32, 32), (32, 16). */
+int sg_conv3d_fwd(int n, int cin, int cout, int mode, const void* in, const void* w, const float* bias,
+                  void* out, const void* mask, void* stream);
+/* Weight and bias gradients: dw[27][cout][cin] = sum_x dZ[x][co] X[x + tap][ci], db[co] = sum_x
+ * dZ[x][co] (float).  ws: caller-owned float workspace of sg_conv3d_wgrad_workspace bytes. */
+int sg_conv3d_wgrad(int n, int cin, int cout, const void* x, const void* dz, float* dw, float* db,
+                    float* ws, size_t ws_bytes, void* stream);
+size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout);
+int sg_last_error(char* buf, int len);
+
 /* Self-test of the erfc used for the per-radius sum of fcoll: writes it (fast) and the CUDA
  * library's erfcf (lib) for n device floats x. */
 int es_selftest_erfc(const float* x, float* fast, float* lib, int n, void* stream);

@@ -1,0 +1,117 @@
+"""Surrogate tensor-core kernels against the float64 CPU oracle, and training (GPU)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import module
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import sg_oracle as SO  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def sg():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import __graft_entry__
+    __graft_entry__.build()
+    return module("surrogate")
+
+
+def _bf(t):
+    return t.to(torch.bfloat16)
+
+
+def _rel(a, b):
+    return ((a - b).norm() / b.norm()).item()
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 32), (32, 32)])
+def test_conv_forward_matches_oracle(sg, cin, cout):
+    n = 32
+    g = torch.Generator().manual_seed(cin + cout)
+    x = torch.randn((n, n, n, cin), generator=g)
+    w = torch.randn((27, cout, cin), generator=g) * 0.1
+    b = torch.randn(cout, generator=g) * 0.1
+    xb, wb = _bf(x), _bf(w)
+    ref = torch.relu(SO.conv3d(xb.double(), wb.double(), b.double()))
+    net = sg.SurrogateNet()
+    out = torch.empty((n, n, n, cout), dtype=torch.bfloat16, device="cuda")
+    net._conv(n, cin, cout, 0, xb.cuda(), wb.cuda(), b.cuda(), out)
+    got = out.float().cpu().double()
+    assert _rel(got, ref) < 4e-3                       # bf16 rounding of the output
+
+
+def test_input_gradient_matches_oracle(sg):
+    n, cin, cout = 32, 32, 32
+    g = torch.Generator().manual_seed(3)
+    xin = torch.relu(torch.randn((n, n, n, cin), generator=g))       # layer input (ReLU output)
+    w = torch.randn((27, cout, cin), generator=g) * 0.1
+    dz = torch.randn((n, n, n, cout), generator=g)
+    wb, dzb, xb = _bf(w), _bf(dz), _bf(xin)
+    x64 = xb.double().requires_grad_(True)
+    y = SO.conv3d(x64, wb.double())
+    y.backward(dzb.double())
+    ref = x64.grad * (xb.double() > 0)
+    net = sg.SurrogateNet()
+    wflip = wb.float().flip(0).transpose(1, 2).contiguous().to(torch.bfloat16)
+    out = torch.empty((n, n, n, cin), dtype=torch.bfloat16, device="cuda")
+    net._conv(n, cout, cin, 2, dzb.cuda(), wflip.cuda(), None, out, mask=xb.cuda())
+    assert _rel(out.float().cpu().double(), ref) < 4e-3
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 32), (32, 32), (32, 16)])
+def test_weight_gradient_matches_oracle(sg, cin, cout):
+    n = 32
+    g = torch.Generator().manual_seed(7 + cin)
+    x = torch.randn((n, n, n, cin), generator=g)
+    dz = torch.randn((n, n, n, cout), generator=g)
+    xb, dzb = _bf(x), _bf(dz)
+    w64 = torch.zeros((27, cout, cin), dtype=torch.float64, requires_grad=True)
+    b64 = torch.zeros(cout, dtype=torch.float64, requires_grad=True)
+    SO.conv3d(xb.double(), w64, b64).backward(dzb.double())
+    net = sg.SurrogateNet()
+    dw = torch.empty((27, cout, cin), device="cuda")
+    db = torch.empty(cout, device="cuda")
+    net._wgrad(n, cin, cout, xb.cuda(), dzb.cuda(), dw, db)
+    assert _rel(dw.cpu().double(), w64.grad) < 1e-5   # fp32 sums of exact bf16 products
+    assert _rel(db.cpu().double(), b64.grad) < 1e-5
+
+
+def test_network_gradients_match_float64_autograd(sg):
+    n = 16
+    net = sg.SurrogateNet(seed=1)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    delta = torch.randn((n, n, n), device="cuda", generator=g) * 0.3
+    target = (torch.rand((n, n, n), device="cuda", generator=g) > 0.5).float()
+    f = sg.features(delta, 8.0, 30.0, 15.0, 2e4)
+    pred, acts = net.forward(f, keep=True)
+    dws, dbs = net.backward(acts, pred, target)
+    ws = [w.to(torch.bfloat16).double().cpu() for w in net.w]
+    rdw, rdb, rpred = SO.net_grads(f.double().cpu(), ws, [b.cpu() for b in net.b], target.cpu())
+    assert _rel(pred.cpu().double(), rpred) < 2e-2
+    for li, (a, r) in enumerate(zip(dws, rdw)):
+        cos = torch.nn.functional.cosine_similarity(a.cpu().double().flatten(), r.flatten(), dim=0).item()
+        assert cos > 0.98, (li, cos)
+
+
+def test_training_beats_the_untrained_network(sg):
+    # engine-generated pairs at 32^3; the trained surrogate must beat its own initialisation and
+    # the constant (mean x_HI) predictor on held-out realisations
+    gen = sg.DataGenerator(n=32, box_len=50.0)
+    rng = np.random.default_rng(0)
+    train = [gen.sample(1000 + i, sg.draw_params(rng)) for i in range(48)]
+    held = [gen.sample(5000 + i, sg.draw_params(rng)) for i in range(8)]
+    net = sg.SurrogateNet(seed=0)
+    before = sg.evaluate(net, held)["mean_abs_dxHI"]
+    losses = sg.train(net, train, epochs=6, lr=3e-3)
+    after = sg.evaluate(net, held)["mean_abs_dxHI"]
+    mean_pred = np.mean([s.xH.mean().item() for s in train])
+    const = np.mean([(s.xH - mean_pred).abs().mean().item() for s in held])
+    assert np.isfinite(losses).all()
+    assert losses[-len(train):].mean() < losses[:len(train)].mean()
+    assert after < before
+    assert after < const
