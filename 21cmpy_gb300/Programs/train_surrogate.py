@@ -1,0 +1,111 @@
+"""Train and evaluate the learned surrogate on pairs generated by the plain engine.
+
+    python -m 21cmpy_gb300.Programs.train_surrogate [--n 128] [--box-len 200] [--train 2048]
+        [--held 128] [--epochs 2] [--lr 2e-3] [--out weights.pt] [--report report.json]
+
+Training pairs: Gaussian random fields of seeds 1000..(1000 + train - 1) at n^3 with parameter
+points drawn uniformly (zeta in [10, 80], R_mfp in [5, 50] Mpc, log10 Tvir in [4, 5.3], z in
+[6, 10]); labels are the plain engine's x_HI.  Evaluation: held-out seeds 5000.. against the plain
+engine (mean |dx_HI|, flag agreement at x_HI = 0.5, P21(k) ratio on k in [0.1, 1] /Mpc), the
+untrained network and the constant mean predictor, plus inference speed in boxes/s next to the
+plain engine's, and a parameter sweep through SurrogateSweep (surrogate with engine fallback).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+import torch
+
+from .. import surrogate as S
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="train_surrogate")
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--box-len", type=float, default=200.0)
+    ap.add_argument("--train", type=int, default=2048)
+    ap.add_argument("--held", type=int, default=128)
+    ap.add_argument("--epochs", type=int, default=2)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--report", default=None)
+    args = ap.parse_args(argv)
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+
+    gen = S.DataGenerator(n=args.n, box_len=args.box_len)
+    rng = np.random.default_rng(args.seed)
+    t0 = time.time()
+    train = [gen.sample(1000 + i, S.draw_params(rng)) for i in range(args.train)]
+    held_rng = np.random.default_rng(args.seed + 1)
+    held = [gen.sample(5000 + i, S.draw_params(held_rng)) for i in range(args.held)]
+    torch.cuda.synchronize()
+    t_data = time.time() - t0
+    log(f"generated {len(train)} + {len(held)} pairs in {t_data:.1f} s")
+
+    net = S.SurrogateNet(seed=args.seed)
+    untrained = S.evaluate(net, held, gen.plan)
+    order_rng = np.random.default_rng(args.seed + 2)
+    t0 = time.time()
+    losses = []
+    for ep in range(args.epochs):
+        perm = order_rng.permutation(len(train))
+        losses.extend(S.train(net, [train[i] for i in perm], epochs=1, lr=args.lr * (0.5 ** ep), log=log))
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    trained = S.evaluate(net, held, gen.plan)
+    mean_pred = float(np.mean([s.xH.mean().item() for s in train]))
+    const_err = float(np.mean([(s.xH - mean_pred).abs().mean().item() for s in held]))
+
+    # inference speed next to the plain engine (inputs resident on the device)
+    s = held[0]
+    f = S.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
+    st = S.schedule.ionize_setup(gen.n, gen.box_len, s.z, zeta=s.zeta, t_vir_min=s.t_vir, R_max=s.R_max,
+                                 cosmo=gen.cosmo, table=gen.table)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        net.forward(f)
+    e0.record()
+    for _ in range(10):
+        net.forward(f)
+    e1.record()
+    e1.synchronize()
+    sg_ms = e0.elapsed_time(e1) / 10
+    for _ in range(3):
+        gen.plan.run(s.delta, st)
+    e0.record()
+    for _ in range(10):
+        gen.plan.run(s.delta, st)
+    e1.record()
+    e1.synchronize()
+    eng_ms = e0.elapsed_time(e1) / 10
+    flop = 2 * gen.n ** 3 * sum(27 * ci * co for ci, co in S.LAYERS)
+
+    sweep = S.SurrogateSweep(net, gen, max_abs_err=0.05, check_every=8)
+    kinds = [sweep(x.delta, dict(z=x.z, zeta=x.zeta, R_max=x.R_max, t_vir=x.t_vir))[1] for x in held]
+    report = {
+        "n": gen.n, "box_len_mpc": gen.box_len, "train_pairs": len(train), "held_out": len(held),
+        "epochs": args.epochs, "data_seconds": t_data, "train_seconds": t_train,
+        "final_bce": float(np.mean(losses[-len(train):])) if losses else None,
+        "trained": trained, "untrained": untrained, "constant_mean_abs_dxHI": const_err,
+        "surrogate_ms_per_box": sg_ms, "surrogate_boxes_per_s": 1e3 / sg_ms,
+        "surrogate_tflops": flop / sg_ms / 1e9,
+        "engine_ms_per_box": eng_ms, "engine_boxes_per_s": 1e3 / eng_ms,
+        "speed_ratio_surrogate_over_engine": eng_ms / sg_ms,
+        "sweep": {"points": len(kinds), "surrogate": kinds.count("surrogate"), "engine": kinds.count("engine")},
+    }
+    print(json.dumps(report), flush=True)
+    if args.report:
+        with open(args.report, "w") as fh:
+            json.dump(report, fh, indent=1)
+    if args.out:
+        torch.save(net.state(), args.out)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
