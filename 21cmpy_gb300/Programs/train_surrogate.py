@@ -1,7 +1,7 @@
 """Train and evaluate the learned surrogate on pairs generated by the plain engine.
 
     python -m 21cmpy_gb300.Programs.train_surrogate [--n 128] [--box-len 200] [--train 2048]
-        [--held 128] [--epochs 2] [--lr 2e-3] [--out weights.pt] [--report report.json]
+        [--held 128] [--epochs 4] [--lr 3e-4] [--out weights.pt] [--report report.json]
 
 Training pairs: Gaussian random fields of seeds 1000..(1000 + train - 1) at n^3 with parameter
 points drawn uniformly (zeta in [10, 80], R_mfp in [5, 50] Mpc, log10 Tvir in [4, 5.3], z in
@@ -29,8 +29,8 @@ def main(argv=None):
     ap.add_argument("--box-len", type=float, default=200.0)
     ap.add_argument("--train", type=int, default=2048)
     ap.add_argument("--held", type=int, default=128)
-    ap.add_argument("--epochs", type=int, default=2)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
@@ -54,7 +54,7 @@ def main(argv=None):
     losses = []
     for ep in range(args.epochs):
         perm = order_rng.permutation(len(train))
-        losses.extend(S.train(net, [train[i] for i in perm], epochs=1, lr=args.lr * (0.5 ** ep), log=log))
+        losses.extend(S.train(net, [train[i] for i in perm], epochs=1, lr=args.lr * (0.7 ** ep), log=log))
     torch.cuda.synchronize()
     t_train = time.time() - t0
     trained = S.evaluate(net, held, gen.plan)

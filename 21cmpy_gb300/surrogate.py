@@ -210,8 +210,11 @@ class DataGenerator:
         return Sample(d, xh.clone(), params["z"], params["zeta"], params["R_max"], params["t_vir"])
 
 
-def train(net: SurrogateNet, samples, epochs: int = 1, lr: float = 2e-3, log=None):
-    """Plain SGD loop over the pairs (one box per step); returns the per-step mean BCE."""
+def train(net: SurrogateNet, samples, epochs: int = 1, lr: float = 3e-4, log=None):
+    """Adam over the pairs, one box per step; returns the per-step mean BCE.
+
+    Step sizes of 2e-3 and above saturate the sigmoid within the first epoch (every output pinned at
+    0 or 1, BCE ~ 9.6); 3e-4 converges on 32^3 and 128^3 pairs."""
     opt = Adam(net.parameters(), lr=lr)
     losses = []
     for ep in range(epochs):
@@ -256,8 +259,10 @@ def evaluate(net: SurrogateNet, samples, plan=None, k_range=(0.1, 1.0), num_bins
 class SurrogateSweep:
     """Parameter sweeps with the surrogate and the plain engine as fallback and judge.
 
-    A point outside the training ranges, or any point when `check_every` samples one out of N for
-    a plain-engine check that fails the error budget, runs the plain engine instead.
+    Every `check_every`-th point also runs the plain engine and records the surrogate's mean |dx_HI|
+    there; a checked point over `max_abs_err` returns the engine's box.  The surrogate stays trusted
+    while the mean error over all checked points is within `max_abs_err`; once it is not, every
+    later point runs the plain engine.  Points outside the training ranges always run the engine.
     """
 
     def __init__(self, net: SurrogateNet, gen: DataGenerator, max_abs_err: float = 0.05, check_every: int = 16):
@@ -265,7 +270,11 @@ class SurrogateSweep:
         self.max_abs_err, self.check_every = max_abs_err, check_every
         self.calls = 0
         self.fallbacks = 0
-        self.trusted = True
+        self.checked = []
+
+    @property
+    def trusted(self) -> bool:
+        return not self.checked or float(np.mean(self.checked)) <= self.max_abs_err
 
     def in_range(self, params):
         lo, hi = PARAM_RANGES["log10_tvir"]
@@ -281,8 +290,9 @@ class SurrogateSweep:
         pred, _ = self.net.forward(features(delta, params["z"], params["zeta"], params["R_max"], params["t_vir"]))
         if self.check_every and self.calls % self.check_every == 0:
             ref = self._engine(delta, params)
-            if (pred - ref).abs().mean().item() > self.max_abs_err:
-                self.trusted = False
+            err = (pred - ref).abs().mean().item()
+            self.checked.append(err)
+            if err > self.max_abs_err:
                 return ref, "engine"
         return pred, "surrogate"
 
