@@ -88,6 +88,9 @@ _PROTOS = {
     "sg_conv3d_wgrad": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_size_t, C.c_void_p]),
     "sg_conv3d_wgrad_workspace": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
+    "sg_conv3d_set_impl": (C.c_int, [C.c_int]),
+    "sg_conv3d_get_impl": (C.c_int, []),
+    "sg_check": (C.c_int, []),
     "sg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_version": (C.c_int, []),

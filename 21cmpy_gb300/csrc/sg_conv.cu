@@ -1,5 +1,6 @@
 // Learned-surrogate kernels: 3x3x3 circular convolutions of channels-last BF16 boxes as implicit
-// GEMMs on the tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulation).
+// GEMMs on the tensor cores (mma.sync m16n8k16, BF16 inputs, FP32 accumulation).  128^3 boxes go
+// to the tcgen05/TMEM kernels of sg_tc.cu unless sg_conv3d_set_impl selects these for every size.
 //
 // Layout: activations [z][y][x][C] bf16 (C contiguous); weights [27][COUT][CIN] bf16 with tap
 // index t = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1).  A CTA computes one output row (z, y): it
@@ -16,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
@@ -291,7 +293,12 @@ int launch_wgrad(int n, const void* x, const void* dz, float* dw, float* db, flo
 }
 
 bool shape_ok(int n) { return n >= 16 && n <= sg::MAXN && n % 16 == 0; }
+std::atomic<int> g_impl{SG_IMPL_AUTO};
 }  // namespace
+
+int sg_tc_conv_fwd(int cin, int cout, int mode, const void* in, const void* w, const float* bias, void* out,
+                   const void* mask, cudaStream_t s, std::string* err);
+int sg_tc_status(unsigned* status);
 
 extern "C" {
 
@@ -300,6 +307,11 @@ int sg_conv3d_fwd(int n, int cin, int cout, int mode, const void* in, const void
   if (!shape_ok(n)) return sgfail(ES_E_ARG, "sg_conv3d_fwd: n=%d must be a multiple of 16 in [16, %d]", n, sg::MAXN);
   if (!in || !w || !out || (mode == sg::DGRAD_MASK && !mask)) return sgfail(ES_E_ARG, "sg_conv3d_fwd: NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
+  if (n == 128 && g_impl.load() == SG_IMPL_AUTO) {
+    std::string err;
+    const int rc = sg_tc_conv_fwd(cin, cout, mode, in, w, bias, out, mask, s, &err);
+    return rc == ES_OK ? ES_OK : sgfail(rc, "sg_conv3d_fwd: %s", err.c_str());
+  }
   if (mode == sg::FWD_RELU) {
     if (cin == 16 && cout == 32) return launch_fwd<16, 32, sg::FWD_RELU>(n, in, w, bias, out, mask, s);
     if (cin == 32 && cout == 32) return launch_fwd<32, 32, sg::FWD_RELU>(n, in, w, bias, out, mask, s);
@@ -330,6 +342,23 @@ size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout) {
   int chunks = (sms * 2 + 8) / 9;
   if (chunks > n * n) chunks = n * n;
   return (size_t)9 * chunks * (27 * cout * cin + cout) * sizeof(float);
+}
+
+int sg_conv3d_set_impl(int impl) {
+  if (impl != SG_IMPL_AUTO && impl != SG_IMPL_MMA_SYNC) return sgfail(ES_E_ARG, "sg_conv3d_set_impl: unknown %d", impl);
+  g_impl.store(impl);
+  return ES_OK;
+}
+
+int sg_conv3d_get_impl(void) { return g_impl.load(); }
+
+int sg_check(void) {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return sgfail(ES_E_CUDA, "sg_check: %s", cudaGetErrorString(e));
+  unsigned st = 0;
+  if (sg_tc_status(&st) != ES_OK) return sgfail(ES_E_CUDA, "sg_check: reading the device status failed");
+  if (st) return sgfail(ES_E_DEVICE, "sg_check: a tcgen05 convolution gave up a bounded wait (status %u)", st);
+  return ES_OK;
 }
 
 int sg_last_error(char* buf, int len) {

@@ -56,6 +56,10 @@ class SurrogateNet:
     def parameters(self):
         return self.w + self.b
 
+    def check(self):
+        """Synchronises; raises if a tcgen05 convolution gave up a bounded wait since the last check."""
+        _lib.check("sg_check", self.lib.sg_check(), self.lib)
+
     def load_state(self, state):
         for i, (w, b) in enumerate(zip(state["w"], state["b"])):
             self.w[i].copy_(w)
@@ -227,6 +231,7 @@ def train(net: SurrogateNet, samples, epochs: int = 1, lr: float = 3e-4, log=Non
             p = pred.clamp(1e-6, 1 - 1e-6)
             loss = -(s.xH * torch.log(p) + (1 - s.xH) * torch.log(1 - p)).mean()
             losses.append(loss)
+        net.check()
         if log:
             log(f"epoch {ep}: mean BCE {torch.stack(losses[-len(samples):]).mean().item():.4f}")
     return torch.stack(losses).cpu().numpy() if losses else np.zeros(0)

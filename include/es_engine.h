@@ -194,6 +194,16 @@ int sg_conv3d_fwd(int n, int cin, int cout, int mode, const void* in, const void
 int sg_conv3d_wgrad(int n, int cin, int cout, const void* x, const void* dz, float* dw, float* db,
                     float* ws, size_t ws_bytes, void* stream);
 size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout);
+/* Which kernels sg_conv3d_fwd runs (process-wide, no counterpart in the reference):
+ * SG_IMPL_AUTO = tcgen05/TMEM kernels for n = 128 (one CTA per SM, TMA-fed, accumulators in tensor
+ * memory) and mma.sync kernels for other n; SG_IMPL_MMA_SYNC = mma.sync kernels for every n. */
+#define SG_IMPL_AUTO 0
+#define SG_IMPL_MMA_SYNC 1
+int sg_conv3d_set_impl(int impl);
+int sg_conv3d_get_impl(void);
+/* Synchronises the device and reports ES_E_DEVICE if a tcgen05 convolution gave up a bounded wait
+ * since the last call (the flag is cleared); ES_OK otherwise. */
+int sg_check(void);
 int sg_last_error(char* buf, int len);
 
 /* Self-test of the erfc used for the per-radius sum of fcoll: writes it (fast) and the CUDA

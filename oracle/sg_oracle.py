@@ -22,6 +22,20 @@ def conv3d(x, w, b=None):
     return y[0].permute(1, 2, 3, 0)
 
 
+def conv3d_planes(x, w, b, planes):
+    """conv3d's output on the z-planes `planes` only: [len(planes), n, n, cout], float64."""
+    n = x.shape[0]
+    outs = []
+    for z in planes:
+        slab = x[[(z - 1) % n, z, (z + 1) % n]].double()          # [3, n, n, cin]
+        xc = slab.permute(3, 0, 1, 2).unsqueeze(0)
+        xc = torch.cat([xc[..., -1:], xc, xc[..., :1]], dim=-1)   # circular in x
+        xc = torch.cat([xc[..., -1:, :], xc, xc[..., :1, :]], dim=-2)  # circular in y
+        y = F.conv3d(xc, _to_conv(w.double()), None if b is None else b.double())
+        outs.append(y[0, :, 0].permute(1, 2, 0))
+    return torch.stack(outs)
+
+
 def net_forward(feats, ws, bs):
     """Hidden layers ReLU, last layer sigmoid of channel 0; returns (pred, activations)."""
     acts = [feats]

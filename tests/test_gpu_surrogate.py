@@ -98,6 +98,75 @@ def test_network_gradients_match_float64_autograd(sg):
         assert cos > 0.98, (li, cos)
 
 
+TC_CASES = [(16, 32, 0), (32, 32, 0), (32, 16, 1), (32, 32, 2), (16, 32, 2)]
+
+
+@pytest.mark.parametrize("cin,cout,mode", TC_CASES)
+def test_tcgen05_conv_matches_oracle_and_mma_sync(sg, cin, cout, mode):
+    # 128^3 runs on the tcgen05/TMEM kernels; the same call with the mma.sync kernels selected and
+    # the float64 oracle on four z-planes (both x edges, both z edges) must agree
+    n = 128
+    lib = sg._lib.load()
+    g = torch.Generator().manual_seed(100 + cin + cout + mode)
+    x = _bf(torch.randn((n, n, n, cin), generator=g))
+    w = _bf(torch.randn((27, cout, cin), generator=g) * 0.1)
+    b = None if mode == 2 else torch.randn(cout, generator=g) * 0.1
+    mask = _bf(torch.relu(torch.randn((n, n, n, cout), generator=g))) if mode == 2 else None
+    shape, dt = ((n, n, n), torch.float32) if mode == 1 else ((n, n, n, cout), torch.bfloat16)
+    net = sg.SurrogateNet()
+    xd, wd = x.cuda(), w.cuda()
+    bd = b.cuda() if b is not None else None
+    md = mask.cuda() if mask is not None else None
+    assert lib.sg_conv3d_get_impl() == 0
+    out_tc = torch.empty(shape, dtype=dt, device="cuda")
+    net._conv(n, cin, cout, mode, xd, wd, bd, out_tc, md)
+    assert lib.sg_check() == 0
+    out_ms = torch.empty(shape, dtype=dt, device="cuda")
+    assert lib.sg_conv3d_set_impl(1) == 0
+    try:
+        net._conv(n, cin, cout, mode, xd, wd, bd, out_ms, md)
+    finally:
+        lib.sg_conv3d_set_impl(0)
+    assert _rel(out_tc.float(), out_ms.float()) < 2e-3   # same products, other summation order
+    planes = [0, 1, 63, 127]
+    ref = SO.conv3d_planes(x.double(), w.double(), b, planes)
+    if mode == 0:
+        ref = torch.relu(ref)
+    elif mode == 1:
+        ref = torch.sigmoid(ref[..., 0])
+    else:
+        ref = ref * (mask[planes].double() > 0)
+    got = out_tc[planes].cpu().double()
+    assert _rel(got, ref) < 4e-3                       # bf16 rounding of the output
+    if mode != 1:
+        assert torch.isfinite(out_tc.float()).all()
+
+
+def test_tcgen05_network_step_matches_mma_sync(sg):
+    # one forward + backward of the full network at 128^3 on both kernel families
+    n = 128
+    lib = sg._lib.load()
+    net = sg.SurrogateNet(seed=2)
+    g = torch.Generator(device="cuda").manual_seed(9)
+    delta = torch.randn((n, n, n), device="cuda", generator=g) * 0.5
+    target = (torch.rand((n, n, n), device="cuda", generator=g) > 0.5).float()
+    f = sg.features(delta, 7.0, 40.0, 20.0, 3e4)
+    res = []
+    for impl in (0, 1):
+        assert lib.sg_conv3d_set_impl(impl) == 0
+        try:
+            pred, acts = net.forward(f, keep=True)
+            dws, dbs = net.backward(acts, pred, target)
+        finally:
+            lib.sg_conv3d_set_impl(0)
+        res.append((pred, dws))
+    assert lib.sg_check() == 0
+    assert _rel(res[0][0], res[1][0]) < 1e-2
+    for li, (a, c) in enumerate(zip(res[0][1], res[1][1])):
+        cos = torch.nn.functional.cosine_similarity(a.flatten().double(), c.flatten().double(), dim=0).item()
+        assert cos > 0.99, (li, cos)
+
+
 def test_training_beats_the_untrained_network(sg):
     # engine-generated pairs at 32^3; the trained surrogate must beat its own initialisation and
     # the constant (mean x_HI) predictor on held-out realisations

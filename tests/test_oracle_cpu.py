@@ -247,3 +247,22 @@ def test_delta_T_factor_matches_reference_formula():
     dT, ave = O.delta_T((1 - g["center_ionized"]).astype(np.float32), g["density"],
                         cos.brightness_temperature_factor(8.0, cos.BASELINE_COSMO))
     assert np.allclose(dT, g["dT"], rtol=1e-12) and ave == pytest.approx(float(g["ave"]), rel=1e-12)
+
+
+def test_surrogate_conv_oracle_planes_and_circular_wrap():
+    torch = pytest.importorskip("torch")
+    from oracle import sg_oracle as SO
+    g = torch.Generator().manual_seed(0)
+    n = 12
+    x = torch.randn((n, n, n, 8), generator=g, dtype=torch.float64)
+    w = torch.randn((27, 4, 8), generator=g, dtype=torch.float64)
+    b = torch.randn(4, generator=g, dtype=torch.float64)
+    full = SO.conv3d(x, w, b)
+    assert torch.allclose(SO.conv3d_planes(x, w, b, [0, 5, n - 1]), full[[0, 5, n - 1]], atol=1e-12)
+    # one voxel by hand: taps reach across every face of the box
+    z, y, xx, co = 0, n - 1, 0, 2
+    s = float(b[co])
+    for t in range(27):
+        dz, dy, dx = t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1
+        s += float((w[t, co] * x[(z + dz) % n, (y + dy) % n, (xx + dx) % n]).sum())
+    assert abs(float(full[z, y, xx, co]) - s) < 1e-10
