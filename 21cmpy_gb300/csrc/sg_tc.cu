@@ -49,7 +49,8 @@ constexpr int YS = 6;                  // input-row groups in the ring
 constexpr int INFLIGHT = 3;            // groups a producer thread keeps in flight (<= YS - 2)
 constexpr int PRODUCERS = 128;         // warps 0..3
 constexpr int MMA_WARP = 4;
-constexpr int THREADS = 288;           // + warp 4 (MMA) + warps 5..8 (epilogue)
+constexpr int EPI_GROUPS = 1;          // epilogue warpgroups, taking output rows in turn
+constexpr int THREADS = 32 * (MMA_WARP + 1 + 4 * EPI_GROUPS);   // + warp 4 (MMA) + warps 5..8 (epilogue)
 constexpr uint32_t TMEM_COLS = 512;
 constexpr long kSpin = 1L << 24;       // mbarrier polls before a wait is declared hung
 constexpr unsigned ERR_TIMEOUT = 1u;
@@ -67,7 +68,6 @@ template <int CIN, int COUT> struct Layout {
   static constexpr int ROW_BYTES = KC * CHUNK;
   static constexpr int RING_BYTES = YS * 3 * ROW_BYTES;
   static constexpr int BAR_OFF = W_BYTES + RING_BYTES;
-  static constexpr int COPIES = 3 * KC * POS;         // 16-byte copies per group
   static constexpr int NBARS = 2 * YS + 2 * S + 1;    // full[YS], sfree[YS], done[S], tfree[S], drain
   static constexpr int BYTES = BAR_OFF + NBARS * 8 + 16 + 128;   // + tmem slot, abort, alignment
   static_assert(W_BYTES % 16 == 0 && ROW_BYTES % 16 == 0, "16-byte aligned regions");
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __nv_bfloat16
   __syncthreads();
   tc_after();
   const uint32_t tmem = *tmem_slot;
-  if (warp > MMA_WARP) {
+  if (warp > MMA_WARP && warp <= MMA_WARP + 4) {
     // every accumulator slot starts at zero
     const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;
     for (int c = 0; c < (int)TMEM_COLS; c += 16) tmem_zero16(tmem + lanes + (uint32_t)c);
@@ -263,7 +263,17 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __nv_bfloat16
 
   if (warp < MMA_WARP) {
     // ------------------------------------------------------------------ copies
+    // Copy j of a row: position p, chunk kc with kc fastest, so a warp reads 8 whole voxels; the
+    // offsets depend only on the thread and j, so they are computed once.
+    constexpr int PER_ROW = KC * POS, JR = (PER_ROW + PRODUCERS - 1) / PRODUCERS;
     const int pt = threadIdx.x;
+    uint32_t soff[JR], goff[JR];
+#pragma unroll
+    for (int j = 0; j < JR; ++j) {
+      const int c = pt + j * PRODUCERS, p = c / KC, kc = c % KC;
+      soff[j] = (uint32_t)(kc * CHUNK + p * 16);
+      goff[j] = (uint32_t)(((p + N - 1) % N) * CIN + kc * 8);
+    }
     int g = 0, published = 0;
     for (int r = rg.r0; r < rg.r1 && !*abort;) {
       const int z = r / N, yb = r % N;
@@ -273,12 +283,13 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __nv_bfloat16
         if (g >= YS && !bar_wait(&sfree[slot], (uint32_t)((g / YS - 1) & 1), abort)) break;
         const int yw = (yy + N) % N;
         unsigned char* gb = ring + slot * 3 * L::ROW_BYTES;
-        // copy c: row d, position p, chunk kc with kc fastest, so a warp reads 8 whole voxels
-        for (int c = pt; c < L::COPIES; c += PRODUCERS) {
-          const int d = c / (KC * POS), rem = c % (KC * POS), p = rem / KC, kc = rem % KC;
-          const int grow = ((z + d + N - 1) % N) * N + yw;
-          const int xv = (p + N - 1) % N;
-          cp_async16(gb + d * L::ROW_BYTES + kc * CHUNK + p * 16, in + ((size_t)grow * N + xv) * CIN + kc * 8);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const __nv_bfloat16* src = in + (size_t)(((z + d + N - 1) % N) * N + yw) * N * CIN;
+          unsigned char* dst = gb + d * L::ROW_BYTES;
+#pragma unroll
+          for (int j = 0; j < JR; ++j)
+            if (PER_ROW % PRODUCERS == 0 || pt + j * PRODUCERS < PER_ROW) cp_async16(dst + soff[j], src + goff[j]);
         }
         cp_async_commit();
         ++g;
@@ -361,8 +372,9 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __nv_bfloat16
     float bv[COUT];
 #pragma unroll
     for (int c = 0; c < COUT; ++c) bv[c] = bias ? bias[c] : 0.f;
-    int o = 0;
-    for (int r = rg.r0; r < rg.r1; ++r, ++o) {
+    const int eg = (warp - MMA_WARP - 1) / 4;         // this warpgroup takes rows o = eg mod EPI_GROUPS
+    for (int o = eg; o < rg.r1 - rg.r0; o += EPI_GROUPS) {
+      const int r = rg.r0 + o;
       const int slot = (S - 1) - o % S;
       const bool ok = bar_wait(&done[slot], (uint32_t)((o / S) & 1), abort);
       if (!__all_sync(0xFFFFFFFFu, ok)) break;        // tcgen05.ld / st need the whole warp
