@@ -2,6 +2,7 @@
 
     python -m 21cmpy_gb300.Programs.train_surrogate [--n 128] [--box-len 200] [--train 2048]
         [--held 128] [--epochs 4] [--lr 3e-4] [--out weights.pt] [--report report.json]
+    python -m 21cmpy_gb300.Programs.train_surrogate --conv-only [--n 128]
 
 Training pairs: Gaussian random fields of seeds 1000..(1000 + train - 1) at n^3 with parameter
 points drawn uniformly (zeta in [10, 80], R_mfp in [5, 50] Mpc, log10 Tvir in [4, 5.3], z in
@@ -34,8 +35,12 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--conv-only", action="store_true",
+                    help="time one 32 -> 32 channel 3^3 convolution layer at n^3 (2 + 3 launches) and exit")
     args = ap.parse_args(argv)
     log = lambda m: print(m, file=sys.stderr, flush=True)
+    if args.conv_only:
+        return conv_only(args.n)
 
     gen = S.DataGenerator(n=args.n, box_len=args.box_len)
     rng = np.random.default_rng(args.seed)
@@ -104,6 +109,30 @@ def main(argv=None):
             json.dump(report, fh, indent=1)
     if args.out:
         torch.save(net.state(), args.out)
+    return 0
+
+
+def conv_only(n: int) -> int:
+    """One 32 -> 32 channel layer on random BF16 activations: two warm-up launches, then three timed
+    ones; prints us / launch."""
+    net = S.SurrogateNet(seed=0)
+    g = torch.Generator(device=net.device).manual_seed(1)
+    x = torch.randn((n, n, n, 32), device=net.device, generator=g).to(torch.bfloat16)
+    w = (torch.randn((27, 32, 32), device=net.device, generator=g) * 0.1).to(torch.bfloat16)
+    b = torch.zeros(32, device=net.device)
+    out = torch.empty_like(x)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(2):
+        net._conv(n, 32, 32, 0, x, w, b, out)
+    e0.record()
+    for _ in range(3):
+        net._conv(n, 32, 32, 0, x, w, b, out)
+    e1.record()
+    e1.synchronize()
+    net.check()
+    us = e0.elapsed_time(e1) / 3 * 1e3
+    print(json.dumps({"n": n, "layer": "32->32", "us_per_launch": us,
+                      "tflops": 2 * n ** 3 * 27 * 32 * 32 / us / 1e6}), flush=True)
     return 0
 
 

@@ -264,10 +264,12 @@ def evaluate(net: SurrogateNet, samples, plan=None, k_range=(0.1, 1.0), num_bins
 class SurrogateSweep:
     """Parameter sweeps with the surrogate and the plain engine as fallback and judge.
 
-    Every `check_every`-th point also runs the plain engine and records the surrogate's mean |dx_HI|
-    there; a checked point over `max_abs_err` returns the engine's box.  The surrogate stays trusted
-    while the mean error over all checked points is within `max_abs_err`; once it is not, every
-    later point runs the plain engine.  Points outside the training ranges always run the engine.
+    Every `check_every`-th point runs both the surrogate and the plain engine and records the
+    surrogate's mean |dx_HI| there; a checked point over `max_abs_err` returns the engine's box.
+    Between checks the surrogate serves the points while the mean error over all checked points is
+    within `max_abs_err`, and the plain engine serves them otherwise; checks go on in both states,
+    so trust lost to an unlucky check comes back.  Points outside the training ranges always run the
+    engine.
     """
 
     def __init__(self, net: SurrogateNet, gen: DataGenerator, max_abs_err: float = 0.05, check_every: int = 16):
@@ -290,10 +292,13 @@ class SurrogateSweep:
 
     def __call__(self, delta: torch.Tensor, params: dict):
         self.calls += 1
-        if not self.in_range(params) or not self.trusted:
+        if not self.in_range(params):
+            return self._engine(delta, params), "engine"
+        check = bool(self.check_every) and self.calls % self.check_every == 0
+        if not check and not self.trusted:
             return self._engine(delta, params), "engine"
         pred, _ = self.net.forward(features(delta, params["z"], params["zeta"], params["R_max"], params["t_vir"]))
-        if self.check_every and self.calls % self.check_every == 0:
+        if check:
             ref = self._engine(delta, params)
             err = (pred - ref).abs().mean().item()
             self.checked.append(err)

@@ -205,6 +205,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven batched-sweep measurement")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-speed measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
@@ -302,6 +303,10 @@ def main():
     if not args.no_batch and world == 1:
         batch_info = run_batch(args, dev)
 
+    surrogate_info = None
+    if not args.no_surrogate and world == 1:
+        surrogate_info = run_surrogate(dev)
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
@@ -330,6 +335,8 @@ def main():
         line["e2e"] = e2e
     if batch_info is not None:
         line["batched_sweep"] = batch_info
+    if surrogate_info is not None:
+        line["surrogate"] = surrogate_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(work, setups, args.cpu_radii)
     if rank == 0:
@@ -378,6 +385,42 @@ def run_e2e(args, work, dev, barrier, dist):
             "d2h_bytes_per_step": nb * (2 * N ** 3 * 4 + 3 * NUM_BINS * 4 + 8),
             "api": "Programs.pipeline.simulate_box (find_HII_bubbles + delta_T on pinned host buffers)",
             "ms_per_step": 1e3 * dt / args.steps}
+
+
+def run_surrogate(dev, reps: int = 20):
+    """Surrogate boxes/s: the network's forward pass on one 128^3 box (tcgen05 convolutions) next to
+    the plain engine (forward FFT + all radii) on the same box, inputs resident on the device."""
+    import torch
+    S = importlib.import_module("21cmpy_gb300.surrogate")
+    gen = S.DataGenerator(n=128, box_len=200.0, device=dev)
+    params = dict(zeta=30.0, R_max=15.0, t_vir=1e4, z=8.0)
+    s = gen.sample(5000, params)
+    st = S.schedule.ionize_setup(gen.n, gen.box_len, s.z, zeta=s.zeta, t_vir_min=s.t_vir, R_max=s.R_max,
+                                 cosmo=gen.cosmo, table=gen.table)
+    net = S.SurrogateNet(seed=0, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    sg_ms = timed(lambda: net.forward(S.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)))
+    eng_ms = timed(lambda: gen.plan.run(s.delta, st))
+    net.check()
+    flop = 2 * gen.n ** 3 * sum(27 * ci * co for ci, co in S.LAYERS)
+    gen.plan.close()
+    return {"workload": "one 128^3 box, BOX_LEN=200 Mpc, z=8, zeta=30, R_mfp=15 Mpc, Tvir=1e4 K",
+            "boxes_per_s": 1e3 / sg_ms, "ms_per_box": sg_ms, "tflops": flop / sg_ms / 1e9,
+            "engine_boxes_per_s": 1e3 / eng_ms, "engine_ms_per_box": eng_ms,
+            "ratio_surrogate_over_engine": eng_ms / sg_ms,
+            "note": "speed with random-init weights (it does not depend on them); accuracy of the trained "
+                    "network against the plain engine is measured by Programs.train_surrogate"}
 
 
 def run_batch(args, dev):

@@ -205,6 +205,11 @@ def test_sweep_uses_the_engine_as_fallback_and_judge(sg):
                                       R_max=p["R_max"], cosmo=gen.cosmo, table=gen.table)
         ref, _ = gen.plan.run(d, st)
         assert torch.equal(xh, ref)
+    # trust lost to a bad check comes back once later checks bring the mean error under budget
+    sweep = sg.SurrogateSweep(net, gen, max_abs_err=1.0, check_every=2)
+    sweep.checked.append(1.2)
+    kinds = [sweep(d, p)[1] for d, p in zip(deltas[:3], pts[:3])]
+    assert kinds == ["engine", "surrogate", "surrogate"], (kinds, sweep.checked)
     # outside the training ranges the surrogate is never asked
     sweep = sg.SurrogateSweep(net, gen, max_abs_err=1.0, check_every=0)
     far = dict(pts[0], zeta=200.0)
