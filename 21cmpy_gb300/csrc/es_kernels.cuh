@@ -50,7 +50,7 @@ struct OpArgs {
   float pk_norm;                  // PRO_PK: V / N^3
   int dimensional;                // PRO_PK: multiply by the mean (DIMENSIONAL_T_POWER_SPEC)
   // col-z inverse filter (times scale, the growth rescale)
-  const float* wtab;              // W(k^2) / N^3 for this radius (synchronous variant)
+  const float* wtab;              // W(k^2) / N^3 for this radius
   float fR;                       // filter radius [Mpc] (TMA variant computes W inline)
   int fk2cut;                     // k-space top-hat cut
   int filter, ref_compat;
@@ -133,7 +133,7 @@ __device__ __forceinline__ bool grid_sum(float mine, float* partials, unsigned* 
 // values (final partial ionisation) use the library erfcf.
 __device__ __forceinline__ float erfc_sum_term(float x) {
   const float z = fabsf(x);
-  const float t = 1.0f / fmaf(0.5f, z, 1.0f);
+  const float t = __fdividef(1.0f, fmaf(0.5f, z, 1.0f));   // divisor in [1, 11]: within 2 ulp
   float p = 0.17087277f;
   p = fmaf(p, t, -0.82215223f);
   p = fmaf(p, t, 1.48851587f);

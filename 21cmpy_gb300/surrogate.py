@@ -125,13 +125,12 @@ def features(delta: torch.Tensor, z: float, zeta: float, R_max: float, t_vir: fl
              cosmo=cosmology.BASELINE_COSMO) -> torch.Tensor:
     """bf16 [n, n, n, 16] network input for a density box at redshift z and a parameter point."""
     n = delta.shape[0]
-    f = torch.zeros((n, n, n, 16), dtype=torch.float32, device=delta.device)
-    f[..., 0] = delta / cosmology.growth_factor(z, cosmo) / 4.0
-    f[..., 1] = zeta / 80.0
-    f[..., 2] = R_max / 50.0
-    f[..., 3] = math.log10(t_vir) - 4.0
-    f[..., 4] = (z - 6.0) / 4.0
-    return f.to(torch.bfloat16)
+    const = torch.zeros(16, dtype=torch.float32)
+    const[1:5] = torch.tensor([zeta / 80.0, R_max / 50.0, math.log10(t_vir) - 4.0, (z - 6.0) / 4.0])
+    f = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=delta.device)
+    f[...] = const.to(device=delta.device, dtype=torch.bfloat16)
+    f[..., 0] = (delta / cosmology.growth_factor(z, cosmo) / 4.0).to(torch.bfloat16)
+    return f
 
 
 class Adam:
