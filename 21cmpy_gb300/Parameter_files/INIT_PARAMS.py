@@ -11,6 +11,7 @@ IO_DIR = "."
 DIM = np.int32(512)                # large (initial-conditions) box, pixels
 HII_DIM = np.int32(128)
 PIXEL_FACTOR = np.float32(DIM) / np.float32(HII_DIM)
+MASS_FACTOR = np.float32(PIXEL_FACTOR ** 3.0)
 BOX_LEN = np.float32(128)
 DELTA_K = np.float32(2 * np.pi / BOX_LEN)
 VOLUME = BOX_LEN * BOX_LEN * BOX_LEN

@@ -11,7 +11,8 @@ from ..Parameter_files import INIT_PARAMS as _P
 
 PARAM_NAMES = ("IO_DIR", "ZETA", "ION_Tvir_MIN", "R_BUBBLE_MAX", "R_BUBBLE_MIN", "DELTA_R_FACTOR",
                "HII_FILTER", "FIND_BUBBLE_ALGORITHM", "COSMO", "NUM_BINS", "DIMENSIONAL_T_POWER_SPEC",
-               "USE_TS_IN_21CM", "DIM")
+               "USE_TS_IN_21CM", "DIM", "HII_DIM", "BOX_LEN", "PIXEL_FACTOR", "MASS_FACTOR", "INITIAL_REDSHIFT",
+               "EVOLVE_DENSITY_LINEARLY")
 
 
 def params(overrides: dict | None = None) -> dict:

@@ -92,6 +92,12 @@ _PROTOS = {
     "sg_conv3d_get_impl": (C.c_int, []),
     "sg_check": (C.c_int, []),
     "sg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
+    "pf_plan_create": (C.c_int, [C.c_int, C.c_int, C.c_float, C.POINTER(C.c_void_p)]),
+    "pf_plan_destroy": (C.c_int, [C.c_void_p]),
+    "pf_move_mass": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float,
+                               C.c_float, C.c_void_p, C.c_void_p]),
+    "pf_evolve_linear": (C.c_int, [C.c_longlong, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p]),
+    "pf_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_version": (C.c_int, []),
 }
@@ -135,10 +141,10 @@ def last_error(lib=None) -> str:
 
 def check(fn: str, code: int, lib=None):
     if code != ES_OK:
-        if fn.startswith("sg_"):
+        if fn.startswith("sg_") or fn.startswith("pf_"):
             lib = lib or load()
             buf = C.create_string_buffer(1024)
-            lib.sg_last_error(buf, len(buf))
+            (lib.sg_last_error if fn.startswith("sg_") else lib.pf_last_error)(buf, len(buf))
             raise EngineError(fn, code, buf.value.decode(errors="replace"))
         if fn.startswith("es_batch"):
             lib = lib or load()

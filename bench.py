@@ -206,6 +206,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven batched-sweep measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-speed measurement")
+    ap.add_argument("--no-perturb", action="store_true", help="skip the density-evolution measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
@@ -306,6 +307,9 @@ def main():
     surrogate_info = None
     if not args.no_surrogate and world == 1:
         surrogate_info = run_surrogate(dev)
+    perturb_info = None
+    if not args.no_perturb and world == 1:
+        perturb_info = run_perturb(dev, hbm)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -337,6 +341,8 @@ def main():
         line["batched_sweep"] = batch_info
     if surrogate_info is not None:
         line["surrogate"] = surrogate_info
+    if perturb_info is not None:
+        line["perturb_field"] = perturb_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(work, setups, args.cpu_radii)
     if rank == 0:
@@ -385,6 +391,55 @@ def run_e2e(args, work, dev, barrier, dist):
             "d2h_bytes_per_step": nb * (2 * N ** 3 * 4 + 3 * NUM_BINS * 4 + 8),
             "api": "Programs.pipeline.simulate_box (find_HII_bubbles + delta_T on pinned host buffers)",
             "ms_per_step": 1e3 * dt / args.steps}
+
+
+def run_perturb(dev, hbm_gbs: float, reps: int = 20):
+    """Zel'dovich move of a 512^3 initial-conditions box onto a 128^3 grid (the reference's default
+    DIM / HII_DIM), inputs resident on the device; L2 is flushed between launches."""
+    import numpy as np
+    import torch
+    pt = importlib.import_module("21cmpy_gb300.perturb")
+    cos = importlib.import_module("21cmpy_gb300.cosmology")
+    dim, sw = 512, 128
+    g = torch.Generator(device=dev).manual_seed(3)
+    d = torch.randn((dim,) * 3, device=dev, generator=g) * 1.5
+    g0 = float(np.float32(cos.growth_factor(300.0, cos.PLANCK13)))
+    ds = float(np.float32((cos.growth_factor(8.0, cos.PLANCK13) - g0) / 128.0))
+    vs = [torch.randn((sw,) * 3, device=dev, generator=g) * (2.0 / sw / ds) for _ in range(3)]
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total = 0.0
+    with pt.PerturbPlan(dim, sw, device=dev) as plan:
+        out = plan.move_mass(d, *vs, init_growth=g0, disp_scale=ds, mass_factor=64.0)
+        for _ in range(3):
+            plan.move_mass(d, *vs, init_growth=g0, disp_scale=ds, mass_factor=64.0, out=out)
+        for _ in range(reps):
+            flush.fill_(1.0)
+            e0.record()
+            plan.move_mass(d, *vs, init_growth=g0, disp_scale=ds, mass_factor=64.0, out=out)
+            e1.record()
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+    ms = total / reps
+    # the oracle (float32 numpy restatement, one thread) on the first 64 DIM planes of the same input
+    po = importlib.import_module("oracle.pf_oracle")
+    dh = d[:64].cpu().numpy()
+    vh = [v.cpu().numpy() for v in vs]
+    t0 = time.perf_counter()
+    po.move_mass(dh, *vh, g0, ds, 4.0, 64.0)
+    cpu_s = time.perf_counter() - t0
+    cpu_rate = dh.size / cpu_s
+    # algorithmic bytes: read deltax once (4 B / DIM cell), the three displacement boxes and the
+    # output once (16 B / HII cell), the accumulator cleared, summed into and read (24 B / HII cell)
+    nbytes = 4.0 * dim ** 3 + 40.0 * sw ** 3
+    gbs = nbytes / (ms / 1e3) / 1e9
+    return {"workload": "Zel'dovich move, DIM=512 -> HII_DIM=128, rms displacement 2 cells (pf_move_mass)",
+            "ms": ms, "cells_per_s": dim ** 3 / (ms / 1e3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs, "unit": "GB/s", "frac": gbs / hbm_gbs,
+                         "bytes_model": "4 B / DIM cell + 40 B / HII cell"},
+            "l2": "flushed (256 MiB write) before every timed launch",
+            "cpu_baseline": {"value": cpu_rate, "unit": "cells/s", "cores": 1, "kind": "port",
+                             "sample": f"64 of 512 DIM planes, numpy float32 oracle, one thread, {cpu_s:.1f} s"}}
 
 
 def run_surrogate(dev, reps: int = 20):

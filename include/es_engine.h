@@ -206,6 +206,23 @@ int sg_conv3d_get_impl(void);
 int sg_check(void);
 int sg_last_error(char* buf, int len);
 
+/* Density evolution producing the excursion-set input boxes (perturb_field.py:39-128).
+ * pf_plan: device tables for a DIM^3 initial-conditions box and an HII_DIM^3 output grid
+ * (pixel_factor = DIM / HII_DIM as float32, INIT_PARAMS.py:7) and the fixed-point accumulator.
+ * pf_move_mass replaces move_mass (perturb_field.cu:90-132) with the velocity scaling and
+ * normalisation around it (perturb_field.py:91-101): delta [DIM^3], vx, vy, vz [HII_DIM^3]
+ * (displacement per unit growth, box-axis order 0, 1, 2), disp_scale = (D(z) - D(z_init)) / BOX_LEN,
+ * init_growth = D(z_init); updated [HII_DIM^3] = mass / mass_factor - 1.  Masses are summed exactly
+ * in 64-bit fixed point (2^-32), so the result does not depend on the order of the atomics.
+ * pf_evolve_linear replaces evolve_linear (perturb_field.py:39-50): out = delta * growth. */
+typedef struct pf_plan pf_plan;
+int pf_plan_create(int dim, int hii_dim, float pixel_factor, pf_plan** plan);
+int pf_plan_destroy(pf_plan* plan);
+int pf_move_mass(pf_plan* plan, const float* delta, const float* vx, const float* vy, const float* vz,
+                 float init_growth, float disp_scale, float mass_factor, float* updated, void* stream);
+int pf_evolve_linear(long long n, const float* delta, float growth, float* out, void* stream);
+int pf_last_error(char* buf, int len);
+
 /* Self-test of the erfc used for the per-radius sum of fcoll: writes it (fast) and the CUDA
  * library's erfcf (lib) for n device floats x. */
 int es_selftest_erfc(const float* x, float* fast, float* lib, int n, void* stream);
