@@ -56,7 +56,7 @@ def build(force: bool = False, jobs: int | None = None) -> Path:
     jobs = jobs or min(len(SIZES) + 1, os.cpu_count() or 4)
     units = [([cc, *ARCH, *FLAGS, f"-DES_N={n}", "-c", str(CSRC / "es_inst.cu"), "-o",
                str(BUILD / f"es_inst_{n}.o")], BUILD / f"es_inst_{n}.o") for n in SIZES]
-    for unit in ("es_engine", "es_batch", "sg_conv", "sg_tc", "pf"):
+    for unit in ("es_engine", "es_batch", "sg_conv", "sg_tc", "pf", "ic"):
         units.append(([cc, *ARCH, *FLAGS, "-c", str(CSRC / f"{unit}.cu"), "-o", str(BUILD / f"{unit}.o")],
                       BUILD / f"{unit}.o"))
     with cf.ThreadPoolExecutor(jobs) as ex:

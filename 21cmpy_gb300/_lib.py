@@ -98,6 +98,12 @@ _PROTOS = {
                                C.c_float, C.c_void_p, C.c_void_p]),
     "pf_evolve_linear": (C.c_int, [C.c_longlong, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p]),
     "pf_last_error": (C.c_int, [C.c_char_p, C.c_int]),
+    "ic_spectrum": (C.c_int, [C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                              C.c_void_p, C.c_void_p]),
+    "ic_shape": (C.c_int, [C.c_int, C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_int, C.c_void_p,
+                           C.c_void_p]),
+    "ic_subsample": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ic_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "es_version": (C.c_int, []),
 }
@@ -141,10 +147,10 @@ def last_error(lib=None) -> str:
 
 def check(fn: str, code: int, lib=None):
     if code != ES_OK:
-        if fn.startswith("sg_") or fn.startswith("pf_"):
+        if fn[:3] in ("sg_", "pf_", "ic_"):
             lib = lib or load()
             buf = C.create_string_buffer(1024)
-            (lib.sg_last_error if fn.startswith("sg_") else lib.pf_last_error)(buf, len(buf))
+            {"sg_": lib.sg_last_error, "pf_": lib.pf_last_error, "ic_": lib.ic_last_error}[fn[:3]](buf, len(buf))
             raise EngineError(fn, code, buf.value.decode(errors="replace"))
         if fn.startswith("es_batch"):
             lib = lib or load()

@@ -310,6 +310,7 @@ def main():
     perturb_info = None
     if not args.no_perturb and world == 1:
         perturb_info = run_perturb(dev, hbm)
+        perturb_info["initial_conditions"] = run_initial(dev)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -440,6 +441,26 @@ def run_perturb(dev, hbm_gbs: float, reps: int = 20):
             "l2": "flushed (256 MiB write) before every timed launch",
             "cpu_baseline": {"value": cpu_rate, "unit": "cells/s", "cores": 1, "kind": "port",
                              "sample": f"64 of 512 DIM planes, numpy float32 oracle, one thread, {cpu_s:.1f} s"}}
+
+
+def run_initial(dev, reps: int = 5):
+    """Initial conditions for DIM = 512, HII_DIM = 128, BOX_LEN = 128 Mpc (the reference's defaults):
+    spectrum, density, smoothed density and three displacement boxes (five 512^3 inverse FFTs)."""
+    import torch
+    ini = importlib.import_module("21cmpy_gb300.initial")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ini.InitialConditions(512, 128, 128.0, device=dev) as ic:
+        normals = ic.normals(0)
+        for _ in range(2):
+            ic.generate(normals=normals)
+        e0.record()
+        for _ in range(reps):
+            ic.generate(normals=normals)
+        e1.record()
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return {"workload": "initial conditions DIM=512, HII_DIM=128, BOX_LEN=128 Mpc: density, smoothed density, "
+                        "3 displacement boxes (5 inverse 512^3 FFTs), normals resident", "ms": ms}
 
 
 def run_surrogate(dev, reps: int = 20):

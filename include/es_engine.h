@@ -223,6 +223,22 @@ int pf_move_mass(pf_plan* plan, const float* delta, const float* vx, const float
 int pf_evolve_linear(long long n, const float* delta, float growth, float* out, void* stream);
 int pf_last_error(char* buf, int len);
 
+/* Initial conditions around the engine's inverse FFT (initialize.py:33-111).  Boxes and half
+ * spectra in numpy rfftn layout ([n][n][n/2+1] complex64), k in units of 2 pi / box_len.
+ * ic_spectrum replaces init_kernel (initialize.cu:58-95) with the complex normals of initialize.py:
+ * 50-56: H = sqrt(P(|k|) box_len^3) (re + i im) / sqrt(2) off the k_z = 0, n/2 planes (without the
+ * 1/sqrt(2) on them), P linear in the table (k_table ascending, k_table[0] below the smallest |k|).
+ * ic_shape replaces HII_filter + set_velocity (initialize.cu:12-40, 148-190): out = W(kR) H
+ * (filter_type -1: no window) times i k_c / k^2 for component c = 0, 1, 2 (-1: density).
+ * ic_subsample replaces subsample (initialize.cu:133-146): small = large[floor(a pf + 0.5)] * scale. */
+int ic_spectrum(int n, float box_len, const float* normals_re, const float* normals_im, const float* k_table,
+                const float* p_table, int table_n, void* out_half, void* stream);
+int ic_shape(int n, float box_len, const void* in_half, int component, int filter_type, float R, int ref_compat,
+             void* out_half, void* stream);
+int ic_subsample(int dim, int hii_dim, float pixel_factor, float scale, const float* large, float* small,
+                 void* stream);
+int ic_last_error(char* buf, int len);
+
 /* Self-test of the erfc used for the per-radius sum of fcoll: writes it (fast) and the CUDA
  * library's erfcf (lib) for n device floats x. */
 int es_selftest_erfc(const float* x, float* fast, float* lib, int n, void* stream);

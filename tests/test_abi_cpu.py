@@ -13,7 +13,7 @@ HEADER = Path(ROOT) / "include" / "es_engine.h"
 
 def declared_functions():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^(?:int|size_t|const char\*)\s+((?:es|sg|pf)_\w+)\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^(?:int|size_t|const char\*)\s+((?:es|sg|pf|ic)_\w+)\(", text, flags=re.M)))
 
 
 @pytest.fixture(scope="module")
