@@ -158,7 +158,8 @@ def cpu_baseline(work, setups, radii: int) -> dict:
 
 
 def run_reference(args):
-    """Reference arm: the oracle port of the path on all host cores (scipy.fft workers)."""
+    """Reference arm: the oracle port of the path on all host cores (scipy.fft workers and a thread
+    pool over slabs for the per-radius elementwise work)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -181,7 +182,7 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     value = N ** 3 * radii * args.steps / dt
     sample = (f"one 256^3 box per step (seed 0, z={s.z}), forward FFT + first {radii} of {st.n_radii} radii, "
-              f"float64 scipy.fft with {cores} workers")
+              f"float64, scipy.fft and the per-radius window / erfc / threshold slabs on {cores} threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",

@@ -166,7 +166,9 @@ def conv_bubbles(deltax, setup, *, tol: float = 1e-5, backend: str = "numpy", wo
       mode);
     * ``means``: per-radius <fcoll> before normalisation.
 
-    ``max_radii`` stops after that many radii (used to time a bounded CPU sample).
+    ``max_radii`` stops after that many radii (used to time a bounded CPU sample).  With
+    ``workers`` > 1 the FFTs use that many threads (scipy backend) and, in centre mode, the window,
+    product and erfc run in slabs on a pool of as many threads (same arithmetic per element).
     """
     rfftn, irfftn = _fft(backend, workers)
     n = setup.n
@@ -186,10 +188,39 @@ def conv_bubbles(deltax, setup, *, tol: float = 1e-5, backend: str = "numpy", wo
     means = []
     ionized = None
     steps = setup.steps if max_radii is None else setup.steps[:max_radii]
+    pool = None
+    if workers > 1 and setup.update == 0:
+        import concurrent.futures as cf
+        pool = cf.ThreadPoolExecutor(workers)
+        slabs = [(a, b) for a, b in zip(np.linspace(0, n, workers + 1).astype(int)[:-1],
+                                        np.linspace(0, n, workers + 1).astype(int)[1:]) if b > a]
     for st in steps:
-        W = window(k2, dk, float(st.R), setup.filter_type, setup.ref_compat) / float(n) ** 3
-        dR = irfftn(X * W, s=(n, n, n), axes=(0, 1, 2)) * float(n) ** 3
-        f = erfc((dc - dR) / float(st.denom))
+        if pool is not None:
+            # the same arithmetic in slabs along axis 0 on all workers (numpy and scipy release the GIL)
+            def shaped(ab, st=st):
+                a, b = ab
+                return X[a:b] * (window(k2[a:b], dk, float(st.R), setup.filter_type, setup.ref_compat) / float(n) ** 3)
+            XW = np.concatenate(list(pool.map(shaped, slabs)))
+            dR = irfftn(XW, s=(n, n, n), axes=(0, 1, 2)) * float(n) ** 3
+
+            def fcoll(ab, st=st):
+                a, b = ab
+                return erfc((dc - dR[a:b]) / float(st.denom))
+            f = np.concatenate(list(pool.map(fcoll, slabs)))
+        else:
+            W = window(k2, dk, float(st.R), setup.filter_type, setup.ref_compat) / float(n) ** 3
+            dR = irfftn(X * W, s=(n, n, n), axes=(0, 1, 2)) * float(n) ** 3
+            f = erfc((dc - dR) / float(st.denom))
+        if pool is not None and not st.final:
+            m = float(sum(pool.map(lambda ab: float(f[ab[0]:ab[1]].sum()), slabs))) / f.size
+            means.append(m)
+            c = float(setup.fc_mean_ps) / m if setup.normalize_mean else 1.0
+
+            def update(ab):
+                a, b = ab
+                np.maximum(max_margin[a:b], zeta * (f[a:b] * c) - 1.0, out=max_margin[a:b])
+            list(pool.map(update, slabs))
+            continue
         m = float(np.mean(f))
         means.append(m)
         if setup.normalize_mean:
@@ -208,6 +239,8 @@ def conv_bubbles(deltax, setup, *, tol: float = 1e-5, backend: str = "numpy", wo
             if setup.update == 0:
                 flags = max_margin >= 0.0
             ionized = np.where(flags, 1.0, np.where(margin >= 0.0, 1.0, zeta * f))
+    if pool is not None:
+        pool.shutdown()
     if setup.update == 0:
         flags = max_margin >= 0.0
         exempt = np.abs(max_margin) <= tol
