@@ -69,3 +69,25 @@ def test_engine_refuses_to_run_without_cuda():
     eng = module("engine")
     with pytest.raises(module("_lib").EngineUnavailable):
         eng.ExcursionSetPlan(64, 100.0)
+
+
+def test_density_evolution_and_initial_condition_arguments_are_checked_without_a_device():
+    _lib = module("_lib")
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.pf_plan_create(64, 32, C.c_float(2.0), None) == -1
+    assert L.pf_plan_create(32, 64, C.c_float(0.5), C.byref(h)) == -1        # HII_DIM above DIM
+    assert L.pf_plan_create(64, 32, C.c_float(1.0), C.byref(h)) == -1        # indices leave the 32^3 grid
+    buf = C.create_string_buffer(256)
+    L.pf_last_error(buf, 256)
+    assert b"leaves the 32^3 grid" in buf.value
+    assert L.pf_move_mass(None, None, None, None, None, C.c_float(0), C.c_float(0), C.c_float(1), None, None) == -1
+    assert L.pf_evolve_linear(-1, None, C.c_float(1), None, None) == -1
+    assert L.pf_evolve_linear(0, None, C.c_float(1), None, None) == 0         # nothing to do
+    assert L.ic_spectrum(1, C.c_float(100.0), None, None, None, None, 512, None, None) == -1
+    assert L.ic_shape(64, C.c_float(100.0), None, 3, 0, C.c_float(1.0), 0, None, None) == -1
+    assert L.ic_subsample(32, 64, C.c_float(0.5), C.c_float(1.0), None, None, None) == -1
+    L.ic_last_error(buf, 256)
+    assert b"ic_subsample" in buf.value
+    with pytest.raises(_lib.EngineError):
+        _lib.check("pf_plan_create", L.pf_plan_create(0, 0, C.c_float(1.0), C.byref(h)), L)
