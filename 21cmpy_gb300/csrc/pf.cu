@@ -39,6 +39,10 @@ constexpr int kWrapLimit = 64;                // box lengths a displacement may 
 __device__ __forceinline__ int target(float p, float vel, float ds, float swf, int sw) {
   float f = __fadd_rn(p, __fmul_rn(vel, ds));
   f = __fmul_rn(f, swf);
+  if (f >= 0.0f && f < swf) {                 // no wrap: the common case
+    const int i = (int)f;
+    return i < sw ? i : sw - 1;
+  }
   if (!isfinite(f)) return 0;
   for (int it = 0; it < kWrapLimit && f >= swf; ++it) f = __fsub_rn(f, swf);
   for (int it = 0; it < kWrapLimit && f < 0.0f; ++it) f = __fadd_rn(f, swf);
@@ -69,13 +73,16 @@ __global__ void __launch_bounds__(256) move_mass_kernel(int dim, int sw, const f
   while (c0 < dim) {
     const int a0 = c0, a1 = c1 * 4 + l1, a2 = c2 * 8 + l2;
     if (a1 < dim && a2 < dim) {
-      const size_t sc = ((size_t)hidx[a0] * sw + hidx[a1]) * sw + hidx[a2];
+      // HII grids up to 1024^3 index in 32 bits; deltax rows are addressed from a 64-bit base
+      const unsigned sc = ((unsigned)hidx[a0] * (unsigned)sw + (unsigned)hidx[a1]) * (unsigned)sw + (unsigned)hidx[a2];
       const int t0 = target(pos[a0], __ldg(vx + sc), ds, swf, sw);
       const int t1 = target(pos[a1], __ldg(vy + sc), ds, swf, sw);
       const int t2 = target(pos[a2], __ldg(vz + sc), ds, swf, sw);
-      const float mass = __fadd_rn(1.0f, __fmul_rn(g0, __ldg(delta + ((size_t)a0 * dim + a1) * dim + a2)));
+      const float* row = delta + ((size_t)a0 * dim + a1) * dim;
+      const float mass = __fadd_rn(1.0f, __fmul_rn(g0, __ldg(row + a2)));
       const long long q = __float2ll_rn(mass * kFix);   // exact scaling by a power of two, then rounding
-      atomicAdd(acc + (((size_t)t0 * sw + t1) * sw + t2), (unsigned long long)q);
+      atomicAdd(acc + (((unsigned)t0 * (unsigned)sw + (unsigned)t1) * (unsigned)sw + (unsigned)t2),
+                (unsigned long long)q);
     }
     c2 += w2;
     if (c2 >= nb2) { c2 -= nb2; ++c1; }
@@ -130,8 +137,9 @@ extern "C" {
 int pf_plan_create(int dim, int hii_dim, float pixel_factor, pf_plan** out) {
   if (!out) return pffail(ES_E_ARG, "pf_plan_create: NULL output");
   *out = nullptr;
-  if (dim < 1 || dim > 2048 || hii_dim < 1 || hii_dim > dim)
-    return pffail(ES_E_ARG, "pf_plan_create: need 1 <= HII_DIM (%d) <= DIM (%d) <= 2048", hii_dim, dim);
+  if (dim < 1 || dim > 2048 || hii_dim < 1 || hii_dim > dim || hii_dim > 1024)
+    return pffail(ES_E_ARG, "pf_plan_create: need 1 <= HII_DIM (%d) <= min(DIM (%d), 1024), DIM <= 2048", hii_dim,
+                  dim);
   if (!(pixel_factor > 0.0f)) return pffail(ES_E_ARG, "pf_plan_create: pixel factor must be positive");
   std::vector<float> pos(dim);
   std::vector<int> hidx(dim);
