@@ -23,6 +23,8 @@ OPT_COL_VARIANT = 1
 OPT_COL_TILE = 2
 OPT_ROW_TILE = 3
 OPT_L2_HINTS = 4
+OPT_COL_RADIX = 5
+OPT_ROW_RADIX = 6
 
 
 class EngineUnavailable(RuntimeError):

@@ -1,9 +1,10 @@
-"""Tile-shape autotuner for the engine's FFT passes.
+"""Tile-shape and radix-schedule autotuner for the engine's FFT passes.
 
 For a box size it times, on the device, every combination of the TMA passes' tile shapes
-(``ES_OPT_COL_TILE`` x ``ES_OPT_ROW_TILE``) plus the synchronous-tile passes, running one
-whole box through the path (forward transform, every radius, final step, delta_T and P(k)), and
-keeps the fastest.  Results are cached per GPU model, box size and library version in a JSON file
+(``ES_OPT_COL_TILE`` x ``ES_OPT_ROW_TILE``) and of the per-radius passes' radix schedules
+(``ES_OPT_COL_RADIX`` x ``ES_OPT_ROW_RADIX``: radices up to 16, or up to 8 with one more stage),
+plus the synchronous-tile passes, running one whole box through the path (forward transform,
+every radius, final step, delta_T and P(k)), and keeps the fastest.  Results are cached per GPU model, box size and library version in a JSON file
 (``$ES_AUTOTUNE_CACHE`` or ``~/.cache/21cmpy_gb300/autotune.json``), so later plans of the same
 size start tuned.
 """
@@ -19,7 +20,9 @@ import torch
 
 from . import _lib, cosmology, schedule
 
-CANDIDATES = [(1, c, r) for c in range(3) for r in range(4)] + [(0, 0, 0)]   # (variant, col tile, row tile)
+# (variant, col tile, row tile, col radix schedule, row radix schedule)
+CANDIDATES = [(1, c, r, cr, rr) for c in range(3) for r in range(4) for cr in range(2) for rr in range(2)] + \
+    [(0, 0, 0, 0, 0)]
 _lock = threading.Lock()
 
 
@@ -52,10 +55,13 @@ def _store(table: dict):
 
 
 def apply(plan, config) -> None:
-    variant, col_tile, row_tile = config
+    config = tuple(config) + (0, 0)[: max(0, 5 - len(config))]    # entries without radix schedules
+    variant, col_tile, row_tile, col_radix, row_radix = config[:5]
     plan.set_option(_lib.OPT_COL_VARIANT, variant)
     plan.set_option(_lib.OPT_COL_TILE, col_tile)
     plan.set_option(_lib.OPT_ROW_TILE, row_tile)
+    plan.set_option(_lib.OPT_COL_RADIX, col_radix)
+    plan.set_option(_lib.OPT_ROW_RADIX, row_radix)
 
 
 def cached(device, n: int):
@@ -101,7 +107,7 @@ def tune(plan, repeats: int = 3, store: bool = True) -> dict:
         best = min(times, key=times.get)
         apply(plan, best)
     result = {"config": list(best), "ms_per_box": times[best],
-              "candidates": {f"{v}/{c}/{r}": round(ms, 4) for (v, c, r), ms in times.items()}}
+              "candidates": {"/".join(map(str, cfg)): round(ms, 4) for cfg, ms in times.items()}}
     if store:
         with _lock:
             table = _load()

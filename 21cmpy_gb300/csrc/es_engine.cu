@@ -106,6 +106,7 @@ struct es_plan {
   CUtensorMap tmX_z, tmX_y, tmXn, tmT_z, tmT_y, tmTn;
   int col_variant = 1;              // passes: 1 TMA double-buffered (default), 0 synchronous
   int col_tile = 0, row_tile = 0;   // TMA tile-shape variants
+  int col_radix = 0, row_radix = 0; // radix schedules of the per-radius passes
   int l2_hints = 1;                 // keep the intermediate spectrum in L2 when it fits
   long l2_bytes = 0;                // device L2 size
   unsigned* err = nullptr;          // device error word (timed-out waits)
@@ -380,6 +381,8 @@ es::OpArgs base_args(const es_plan* p) {
   a.variant = p->col_variant;
   a.col_tile = p->col_tile;
   a.row_tile = p->row_tile;
+  a.col_radix = p->col_radix;
+  a.row_radix = p->row_radix;
   a.scale = 1.0f;
   return a;
 }
@@ -474,7 +477,7 @@ int forward_into(es_plan* p, const float* in, float scale, bool into_T, cudaStre
 
 extern "C" {
 
-int es_version(void) { return 1; }
+int es_version(void) { return 2; }
 
 int es_last_error(char* buf, int len) {
   if (!buf || len <= 0) return ES_E_ARG;
@@ -861,6 +864,11 @@ int es_plan_set_option(es_plan* p, int option, int value) {
       if (value != 0 && value != 1) return fail(ES_E_ARG, "es_plan_set_option: L2 hints must be 0 or 1");
       p->l2_hints = value;
       return ES_OK;
+    case ES_OPT_COL_RADIX:
+    case ES_OPT_ROW_RADIX:
+      if (value != 0 && value != 1) return fail(ES_E_ARG, "es_plan_set_option: radix schedule must be 0 or 1");
+      (option == ES_OPT_COL_RADIX ? p->col_radix : p->row_radix) = value;
+      return ES_OK;
     default:
       return fail(ES_E_ARG, "es_plan_set_option: unknown option %d", option);
   }
@@ -873,6 +881,8 @@ int es_plan_get_option(es_plan* p, int option, int* value) {
     case ES_OPT_COL_TILE: *value = p->col_tile; return ES_OK;
     case ES_OPT_ROW_TILE: *value = p->row_tile; return ES_OK;
     case ES_OPT_L2_HINTS: *value = p->l2_hints; return ES_OK;
+    case ES_OPT_COL_RADIX: *value = p->col_radix; return ES_OK;
+    case ES_OPT_ROW_RADIX: *value = p->row_radix; return ES_OK;
     default: return fail(ES_E_ARG, "es_plan_get_option: unknown option %d", option);
   }
 }

@@ -115,38 +115,51 @@ template <bool INV> struct Dft<16, INV> {
 };
 
 // ---------------------------------------------------------------- radix plans per line length
-template <int N> struct Plan;
-#define ES_PLAN(NN, ...)                                                   \
-  template <> struct Plan<NN> {                                            \
+// RS selects the radix schedule: 0 = fewest stages (radix up to 16), 1 = radices up to 8 (one more
+// stage where that differs; smaller butterflies, fewer registers per thread).
+template <int N, int RS = 0> struct Plan;
+#define ES_PLAN(NN, RSV, ...)                                              \
+  template <> struct Plan<NN, RSV> {                                       \
     static constexpr int radix[] = {__VA_ARGS__};                          \
     static constexpr int stages = sizeof(radix) / sizeof(int);             \
   };
-ES_PLAN(16, 16)
-ES_PLAN(24, 8, 3)
-ES_PLAN(32, 8, 4)
-ES_PLAN(48, 16, 3)
-ES_PLAN(64, 8, 8)
-ES_PLAN(80, 16, 5)
-ES_PLAN(96, 8, 4, 3)
-ES_PLAN(128, 16, 8)
-ES_PLAN(160, 8, 4, 5)
-ES_PLAN(256, 16, 16)
-ES_PLAN(512, 8, 8, 8)
+ES_PLAN(16, 0, 16)
+ES_PLAN(24, 0, 8, 3)
+ES_PLAN(32, 0, 8, 4)
+ES_PLAN(48, 0, 16, 3)
+ES_PLAN(64, 0, 8, 8)
+ES_PLAN(80, 0, 16, 5)
+ES_PLAN(96, 0, 8, 4, 3)
+ES_PLAN(128, 0, 16, 8)
+ES_PLAN(160, 0, 8, 4, 5)
+ES_PLAN(256, 0, 16, 16)
+ES_PLAN(512, 0, 8, 8, 8)
+ES_PLAN(16, 1, 4, 4)
+ES_PLAN(24, 1, 8, 3)
+ES_PLAN(32, 1, 4, 8)
+ES_PLAN(48, 1, 4, 4, 3)
+ES_PLAN(64, 1, 4, 4, 4)
+ES_PLAN(80, 1, 4, 4, 5)
+ES_PLAN(96, 1, 8, 4, 3)
+ES_PLAN(128, 1, 8, 4, 4)
+ES_PLAN(160, 1, 8, 4, 5)
+ES_PLAN(256, 1, 8, 8, 4)
+ES_PLAN(512, 1, 8, 8, 8)
 #undef ES_PLAN
 
-template <int N, int S> struct StageNs {                 // product of the radices before stage S
-  static constexpr int value = StageNs<N, S - 1>::value * Plan<N>::radix[S - 1];
+template <int N, int S, int RS = 0> struct StageNs {      // product of the radices before stage S
+  static constexpr int value = StageNs<N, S - 1, RS>::value * Plan<N, RS>::radix[S - 1];
 };
-template <int N> struct StageNs<N, 0> { static constexpr int value = 1; };
+template <int N, int RS> struct StageNs<N, 0, RS> { static constexpr int value = 1; };
 
 // Lines of length N in shared memory: element e of line l at buf[l * LS + e * ES].
 // LINE_FAST maps consecutive threads to consecutive lines (column tiles), otherwise to
 // consecutive butterflies of one line (row tiles).  tw[m] = w_TWN^m with TWN a multiple of N.
-template <int N, int S, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN>
+template <int N, int S, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN, int RS = 0>
 __device__ __forceinline__ void stockham_stage(const float2* __restrict__ in, float2* __restrict__ out,
                                                const float2* __restrict__ tw) {
-  constexpr int R = Plan<N>::radix[S];
-  constexpr int Ns = StageNs<N, S>::value;
+  constexpr int R = Plan<N, RS>::radix[S];
+  constexpr int Ns = StageNs<N, S, RS>::value;
   constexpr int NB = NL * (N / R);
   for (int b = threadIdx.x; b < NB; b += T) {
     int l, j;
@@ -171,24 +184,25 @@ __device__ __forceinline__ void stockham_stage(const float2* __restrict__ in, fl
   }
 }
 
-template <int N, int S, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN>
+template <int N, int S, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN, int RS = 0,
+          bool LAST = (S == Plan<N, RS>::stages)>
 struct Stages {
   // runs stages S.. and returns the buffer that holds the result
   static __device__ __forceinline__ float2* run(float2* a, float2* b, const float2* tw) {
-    stockham_stage<N, S, INV, NL, T, LINE_FAST, ES, LS, TWN>(a, b, tw);
+    stockham_stage<N, S, INV, NL, T, LINE_FAST, ES, LS, TWN, RS>(a, b, tw);
     __syncthreads();
-    return Stages<N, S + 1, INV, NL, T, LINE_FAST, ES, LS, TWN>::run(b, a, tw);
+    return Stages<N, S + 1, INV, NL, T, LINE_FAST, ES, LS, TWN, RS>::run(b, a, tw);
   }
 };
-template <int N, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN>
-struct Stages<N, Plan<N>::stages, INV, NL, T, LINE_FAST, ES, LS, TWN> {
+template <int N, int S, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN, int RS>
+struct Stages<N, S, INV, NL, T, LINE_FAST, ES, LS, TWN, RS, true> {
   static __device__ __forceinline__ float2* run(float2* a, float2*, const float2*) { return a; }
 };
 
 // Full line FFT, ping-ponging between a and b; the caller synchronises before it.
-template <int N, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN>
+template <int N, bool INV, int NL, int T, bool LINE_FAST, int ES, int LS, int TWN, int RS = 0>
 __device__ __forceinline__ float2* fft_lines(float2* a, float2* b, const float2* tw) {
-  return Stages<N, 0, INV, NL, T, LINE_FAST, ES, LS, TWN>::run(a, b, tw);
+  return Stages<N, 0, INV, NL, T, LINE_FAST, ES, LS, TWN, RS>::run(a, b, tw);
 }
 
 // bit spread: 16-bit x -> 32-bit word with x's bits at the even positions

@@ -29,12 +29,21 @@ static cudaError_t launch(int smem, const OpArgs& a, int threads, cudaStream_t s
   return cudaGetLastError();
 }
 
+template <int N, int MODE, int RS>
+static cudaError_t launch_col_tma(const OpArgs& a, cudaStream_t s) {
+  if (a.col_tile == 1) return launch<col_tma<N, MODE, 1, RS>>(TmaSmem<N, MODE, 1>::bytes, a, ColTile<N, 1>::T, s);
+  if (a.col_tile == 2) return launch<col_tma<N, MODE, 2, RS>>(TmaSmem<N, MODE, 2>::bytes, a, ColTile<N, 2>::T, s);
+  return launch<col_tma<N, MODE, 0, RS>>(TmaSmem<N, MODE, 0>::bytes, a, ColTile<N, 0>::T, s);
+}
+
+// The per-radius column passes also come with the small-radix schedule (ES_OPT_COL_RADIX).
 template <int N, int MODE>
 static cudaError_t launch_col(const OpArgs& a, cudaStream_t s) {
   if (a.variant == 0) return launch<col_pass<N, MODE>>(ColSmem<N, MODE>::bytes, a, ColCfg<N>::T, s);
-  if (a.col_tile == 1) return launch<col_tma<N, MODE, 1>>(TmaSmem<N, MODE, 1>::bytes, a, ColTile<N, 1>::T, s);
-  if (a.col_tile == 2) return launch<col_tma<N, MODE, 2>>(TmaSmem<N, MODE, 2>::bytes, a, ColTile<N, 2>::T, s);
-  return launch<col_tma<N, MODE, 0>>(TmaSmem<N, MODE, 0>::bytes, a, ColTile<N, 0>::T, s);
+  if constexpr (MODE == COL_Z_INV_FILTER || MODE == COL_Y_INV) {
+    if (a.col_radix == 1) return launch_col_tma<N, MODE, 1>(a, s);
+  }
+  return launch_col_tma<N, MODE, 0>(a, s);
 }
 
 template <int N, int PRO>
@@ -48,16 +57,25 @@ static cudaError_t launch_r2c(const OpArgs& a, cudaStream_t s) {
   }
 }
 
+template <int N, int EPI, int RS>
+static cudaError_t launch_c2r_tma(const OpArgs& a, cudaStream_t s) {
+  constexpr bool P = EPI == EPI_IONIZE;
+  switch (a.row_tile) {
+    case 1: return launch<row2_c2r<N, EPI, 1, RS>>(Row2Smem<N, P, 1>::bytes, a, RowTile<N, 1>::T, s);
+    case 2: return launch<row2_c2r<N, EPI, 2, RS>>(Row2Smem<N, P, 2>::bytes, a, RowTile<N, 2>::T, s);
+    case 3: return launch<row2_c2r<N, EPI, 3, RS>>(Row2Smem<N, P, 3>::bytes, a, RowTile<N, 3>::T, s);
+    default: return launch<row2_c2r<N, EPI, 0, RS>>(Row2Smem<N, P, 0>::bytes, a, RowTile<N, 0>::T, s);
+  }
+}
+
+// The per-radius row pass also comes with the small-radix schedule (ES_OPT_ROW_RADIX).
 template <int N, int EPI>
 static cudaError_t launch_c2r(const OpArgs& a, cudaStream_t s) {
-  constexpr bool P = EPI == EPI_IONIZE;
   if (a.variant == 0) return launch<row_c2r<N, EPI>>(RowSmem<N>::bytes, a, RowCfg<N>::T, s);
-  switch (a.row_tile) {
-    case 1: return launch<row2_c2r<N, EPI, 1>>(Row2Smem<N, P, 1>::bytes, a, RowTile<N, 1>::T, s);
-    case 2: return launch<row2_c2r<N, EPI, 2>>(Row2Smem<N, P, 2>::bytes, a, RowTile<N, 2>::T, s);
-    case 3: return launch<row2_c2r<N, EPI, 3>>(Row2Smem<N, P, 3>::bytes, a, RowTile<N, 3>::T, s);
-    default: return launch<row2_c2r<N, EPI, 0>>(Row2Smem<N, P, 0>::bytes, a, RowTile<N, 0>::T, s);
+  if constexpr (EPI == EPI_IONIZE) {
+    if (a.row_radix == 1) return launch_c2r_tma<N, EPI, 1>(a, s);
   }
+  return launch_c2r_tma<N, EPI, 0>(a, s);
 }
 
 template <int N>

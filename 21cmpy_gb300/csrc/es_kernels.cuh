@@ -32,6 +32,7 @@ struct OpArgs {
   unsigned* err;                  // device error word (bounded waits that timed out)
   int variant;                    // passes: 0 synchronous tiles, 1 TMA double-buffered
   int col_tile, row_tile;         // TMA tile-shape variants (chosen by the autotuner)
+  int col_radix, row_radix;       // radix schedules of the per-radius passes (0: up to 16, 1: up to 8)
   int hint_in, hint_out;          // L2 policies of the TMA loads / stores (ES_HINT_*)
   int discard_in;                 // row pass: drop the consumed input lines from L2
   int grid;                       // CTAs to launch (persistent grid-stride)

@@ -40,7 +40,7 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
 }
 
 // Half-spectrum rows -> real rows with the excursion-set epilogue (EPI_IONIZE) or a plain store.
-template <int N, int EPI, int V>
+template <int N, int EPI, int V, int RS = 0>
 __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2r(const __grid_constant__ OpArgs a) {
   constexpr int M = N / 2, RL = RowTile<N, V>::RL, T = RowTile<N, V>::T, ES = RL + 1;
   constexpr bool PREV = EPI == EPI_IONIZE;
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
       for (int l = threadIdx.x; l < (int)(tile_bytes / 128); l += T) l2_discard(g + 128 * l);
     }
     __syncthreads();
-    float2* Zr = fft_lines<M, true, RL, T, true, ES, 1, N>(A, B, tw);
+    float2* Zr = fft_lines<M, true, RL, T, true, ES, 1, N, RS>(A, B, tw);
     if (EPI == EPI_STORE) {
       for (int e = threadIdx.x; e < RL * M; e += T) {
         const int row = e / M, p = e % M;

@@ -84,10 +84,10 @@ __device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.
 __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Stage 0 of a line FFT with a hook applied to every loaded element (filter, column packing).
-template <int N, bool INV, int NL, int T, int ES, int TWN, class Pre>
+template <int N, bool INV, int NL, int T, int ES, int TWN, int RS, class Pre>
 __device__ __forceinline__ void stockham_stage0_pre(const float2* __restrict__ in, float2* __restrict__ out,
                                                     const float2* __restrict__ tw, Pre pre) {
-  constexpr int R = Plan<N>::radix[0];
+  constexpr int R = Plan<N, RS>::radix[0];
   constexpr int NB = NL * (N / R);
   for (int b = threadIdx.x; b < NB; b += T) {
     const int l = b % NL, j = b / NL;
@@ -100,11 +100,11 @@ __device__ __forceinline__ void stockham_stage0_pre(const float2* __restrict__ i
   }
 }
 
-template <int N, bool INV, int NL, int T, int ES, int TWN, class Pre>
+template <int N, bool INV, int NL, int T, int ES, int TWN, int RS, class Pre>
 __device__ __forceinline__ float2* fft_columns_pre(float2* a, float2* b, const float2* tw, Pre pre) {
-  stockham_stage0_pre<N, INV, NL, T, ES, TWN>(a, b, tw, pre);
+  stockham_stage0_pre<N, INV, NL, T, ES, TWN, RS>(a, b, tw, pre);
   __syncthreads();
-  return Stages<N, 1, INV, NL, T, true, ES, 1, TWN>::run(b, a, tw);
+  return Stages<N, 1, INV, NL, T, true, ES, 1, TWN, RS>::run(b, a, tw);
 }
 
 // TMA column-pass tile shapes: variant 0 = (TI columns, T threads) of the synchronous pass,
@@ -173,14 +173,14 @@ template <int N, int MODE, int V> struct TmaSmem {
   static constexpr int bytes = 3 * tile + N * 8 + pk + 16 + 128;
 };
 
-template <int N, int MODE, int V>
+template <int N, int MODE, int V, int RS = 0>
 __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma(const __grid_constant__ OpArgs a) {
   constexpr int M = N / 2;
   constexpr int TI = ColTile<N, V>::TI, T = ColTile<N, V>::T;
   constexpr bool INV = (MODE == COL_Z_INV_FILTER || MODE == COL_Y_INV || MODE == COL_Z_INV);
   constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
   constexpr int CPR = M / TI;
-  constexpr bool RESULT_IN_W = (Plan<N>::stages % 2) == 1;
+  constexpr bool RESULT_IN_W = (Plan<N, RS>::stages % 2) == 1;
   const int ntiles = ZPASS ? N * CPR + N / TI : N * CPR;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -238,13 +238,13 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
 
     float2* out;
     if (MODE == COL_Z_INV_FILTER) {
-      out = fft_columns_pre<N, INV, TI, T, TI, N>(S, W, tw, [&](int col, int k, float2 v) {
+      out = fft_columns_pre<N, INV, TI, T, TI, N, RS>(S, W, tw, [&](int col, int k, float2 v) {
         return cscale(v, wcol[col * (M + 1) + (k > M ? N - k : k)]);
       });
     } else if (MODE == COL_Y_INV) {
       const float2* nyq = a.cin_nyq + (size_t)t.plane * N;
       const bool pack = t.c == 0;
-      out = fft_columns_pre<N, INV, TI, T, TI, N>(S, W, tw, [&](int col, int j, float2 v) {
+      out = fft_columns_pre<N, INV, TI, T, TI, N, RS>(S, W, tw, [&](int col, int j, float2 v) {
         if (pack && col == 0) {                      // u = y0 + i yM (both Hermitian columns)
           const float2 ym = nyq[j];
           v = make_float2(v.x - ym.y, v.y + ym.x);
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
         return v;
       });
     } else {
-      out = fft_columns_pre<N, INV, TI, T, TI, N>(S, W, tw, [](int, int, float2 v) { return v; });
+      out = fft_columns_pre<N, INV, TI, T, TI, N, RS>(S, W, tw, [](int, int, float2 v) { return v; });
     }
     (void)RESULT_IN_W;
 

@@ -338,7 +338,7 @@ def main():
                    "parallelism": f"{world} independent GPU(s), boxes sharded by seed, no collective"},
         "gpu_launches": int(sum(c for _ms, c in prof.values())),
         "autotune": {"config": tuned.get("config"), "source": tuned.get("source"),
-                     "meaning": "(pass variant, column tile, row tile)"},
+                     "meaning": "(pass variant, column tile, row tile, column radix schedule, row radix schedule)"},
         "kernel_ms": {k: round(v[0], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "kernel_ms_note": f"per-launch CUDA events over a second pass of the same {args.steps} steps "
                           f"({1e3 * elapsed_profiled / args.steps:.1f} ms per step with the events)",

@@ -74,6 +74,12 @@ int es_supported_sizes(int* sizes, int cap);
 /* ES_OPT_L2_HINTS (default 1): keep the intermediate spectrum in L2 between the passes of a
  * radius when it fits (cache-policy hints on the TMA copies, consumed lines discarded). */
 #define ES_OPT_L2_HINTS 4
+/* ES_OPT_COL_RADIX / ES_OPT_ROW_RADIX (default 0): radix schedule of the per-radius TMA column
+ * passes (z inverse + filter, y inverse) and of the row pass (C2R + ionise): 0 = fewest stages with
+ * radices up to 16 (e.g. 16 x 16 for 256 points), 1 = radices up to 8 (8 x 8 x 4).  Chosen by the
+ * autotuner with the tile shapes. */
+#define ES_OPT_COL_RADIX 5
+#define ES_OPT_ROW_RADIX 6
 int es_plan_set_option(es_plan* plan, int option, int value);
 int es_plan_get_option(es_plan* plan, int option, int* value);
 /* Synchronises the stream and reports ES_E_DEVICE if any kernel of the plan gave up a bounded
