@@ -9,11 +9,13 @@ Same inputs and outputs as the reference (perturb_field.py:39-148), under IO_DIR
 * Zel'dovich: ``deltax_z0.00_{DIM}_{L}Mpc.npy`` moved by ``v{x,y,z}overddot_{HII_DIM}_{L}Mpc.npy``
   times (D(z) - D(INITIAL_REDSHIFT)) / BOX_LEN onto the HII_DIM^3 grid (mass / MASS_FACTOR - 1);
 
-both written as ``updated_smoothed_deltax_z{z:.2f}_{HII_DIM}_{L}Mpc.npy``.  The compute runs on the
-GPU (``pf_evolve_linear``, ``pf_move_mass``); D(z) is the Carroll-Press-Turner growth normalised to
-1 at z = 0 (cosmolopy's ``fgrowth``), computed on the host in double and rounded to float32 as the
-reference's np.float32 does.  The reference's recomputed velocity boxes (``updated_v*overddot``,
-perturb_field.py:103-113, used only with T_USE_VELOCITIES) are not produced.
+both written as ``updated_smoothed_deltax_z{z:.2f}_{HII_DIM}_{L}Mpc.npy``.  After a Zel'dovich move
+the velocity boxes at z are recomputed from the DIM^3 density (perturb_field.py:110-125) and written
+as ``updated_v{x,y,z}overddot_{HII_DIM}_{L}Mpc.npy`` (cMpc/s).  The compute runs on the GPU
+(``pf_evolve_linear``, ``pf_move_mass``, the engine's real FFTs with ``ic_shape`` and
+``ic_subsample``); D(z) is the Carroll-Press-Turner growth normalised to 1 at z = 0 (cosmolopy's
+``fgrowth``) and dD/dt / D its rate (``dDdtoverD``), computed on the host in double and rounded to
+float32 as the reference's np.float32 does.
 """
 from __future__ import annotations
 
@@ -62,8 +64,38 @@ def evolve_linear(z, deltax, *, params=None, device=None, save=True):
     return updated
 
 
-def evolve_zeldovich(z, deltax, vx=None, vy=None, vz=None, *, params=None, device=None, save=True):
-    """First-order Zel'dovich move of the DIM^3 box onto the HII_DIM^3 grid (perturb_field.py:52-101).
+def velocity_name(component: str, p) -> str:
+    """perturb_field.py:126."""
+    return "updated_v{0}overddot_{1:d}_{2:.0f}Mpc".format(component, int(p["HII_DIM"]), float(p["BOX_LEN"]))
+
+
+def evolve_velocities(z, deltax, *, params=None, device=None, save=True, hii_dim=None):
+    """Velocity boxes at z from the DIM^3 density at z = 0 (perturb_field.py:110-125): returns
+    {"vx", "vy", "vz"} host arrays of shape HII_DIM^3, in cMpc/s."""
+    import torch
+    from .. import perturb
+    p = _common.params(params)
+    hii = int(p["HII_DIM"]) if hii_dim is None else int(hii_dim)
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    d, _ = _common.to_device(deltax, dev)
+    dim = int(d.shape[0])
+    pf = np.float32(p["PIXEL_FACTOR"]) if dim == int(p["DIM"]) and hii == int(p["HII_DIM"]) else \
+        np.float32(dim) / np.float32(hii)
+    rate = np.float32(cosmology.growth_rate(float(z), _common.cosmo_of(p)))       # perturb_field.py:117
+    vs = perturb.updated_velocities(d, hii, float(p["BOX_LEN"]), float(rate), pixel_factor=float(pf))
+    out = {k: v.cpu().numpy() for k, v in vs.items()}
+    if save:
+        q = dict(p, HII_DIM=hii)
+        for c in ("x", "y", "z"):
+            np.save(os.path.join(_boxes(p), velocity_name(c, q)), out["v" + c])
+    return out
+
+
+def evolve_zeldovich(z, deltax, vx=None, vy=None, vz=None, *, params=None, device=None, save=True,
+                     velocities=True):
+    """First-order Zel'dovich move of the DIM^3 box onto the HII_DIM^3 grid (perturb_field.py:52-101),
+    then, with ``velocities``, the velocity boxes at z (perturb_field.py:110-125, written when
+    ``save``).
 
     vx, vy, vz: the initial-conditions displacement boxes (v / D-dot, HII_DIM^3, box-axis order
     0, 1, 2); read from IO_DIR/Boxes like the reference when not given."""
@@ -100,6 +132,13 @@ def evolve_zeldovich(z, deltax, vx=None, vy=None, vz=None, *, params=None, devic
         plan.close()
     if save:
         np.save(os.path.join(_boxes(p), output_name(z, dict(p, HII_DIM=hii))), updated)
+    if velocities:
+        from ..engine import supported_sizes
+        if dim in supported_sizes():
+            evolve_velocities(z, d, params=params, device=dev, save=save, hii_dim=hii)
+        else:
+            print("perturb_field: WARNING: no velocity boxes: the GPU FFT has no {0}^3 size (supported: {1})"
+                  .format(dim, supported_sizes()), file=sys.stderr)
     return updated
 
 

@@ -16,6 +16,8 @@ the ``cosmo_files/sigmas.py`` integrator that the reference path uses:
   with sigma_8 normalisation; transfer function BBKS (Bardeen et al. 1986, eq. G3, with the
   Sugiyama 1995 shape parameter) or the Eisenstein & Hu (1998) zero-baryon fit, eqs. 26-31.
 * ``pb.fgrowth`` -> :func:`growth_factor`: Carroll, Press & Turner (1992) eq. 29.
+* ``dDdtoverD`` (Programs/cosmo_functions.py:7-21, on cosmolopy's ``fgrowth`` and ``age``) ->
+  :func:`growth_rate`, with :func:`hubble` for H(z).
 * ``pb.virial_mass`` -> :func:`virial_mass`: Barkana & Loeb (2001) eq. 26, with the 21cmFAST
   mean molecular weight convention (0.59 at T >= 1e4 K, 1.22 below).
 
@@ -31,12 +33,14 @@ import numpy as np
 
 __all__ = [
     "Cosmology", "PLANCK13", "BASELINE_COSMO", "transfer_bbks", "transfer_eh_nowiggle",
-    "power_spectrum_z0", "growth_factor", "virial_mass", "mass_to_radius", "SigmaTable",
+    "power_spectrum_z0", "growth_factor", "growth_rate", "hubble", "virial_mass", "mass_to_radius", "SigmaTable",
     "sig_del", "collapse_fraction", "tophat_window", "brightness_temperature_factor",
 ]
 
 # critical density today in h^2 Msun / Mpc^3 (3 H0^2 / 8 pi G with H0 = 100 h km/s/Mpc)
 RHO_CRIT_H2 = 2.77536627e11
+# kilometres per megaparsec (IAU 2012 astronomical unit; parsec = 648000 / pi au)
+MPC_KM = 3.0856775814913673e19
 
 
 @dataclass(frozen=True)
@@ -164,6 +168,23 @@ def growth_factor(z: float, cosmo: Cosmology) -> float:
         om, ol = _omegas_z(zz, cosmo)
         return 2.5 * om / (om ** (4.0 / 7.0) - ol + (1.0 + om / 2.0) * (1.0 + ol / 70.0))
     return g(z) / (g(0.0) * (1.0 + z))
+
+
+def hubble(z: float, cosmo: Cosmology) -> float:
+    """H(z) in 1/s: 100 h km/s/Mpc times sqrt(Om (1+z)^3 + Ok (1+z)^2 + OL)."""
+    a1 = 1.0 + z
+    e2 = cosmo.omega_M_0 * a1 ** 3 + cosmo.omega_k_0 * a1 ** 2 + cosmo.omega_lambda_0
+    return 100.0 * cosmo.h / MPC_KM * math.sqrt(e2)
+
+
+def growth_rate(z: float, cosmo: Cosmology, dz: float = 1e-4) -> float:
+    """(dD/dt) / D in 1/s (Programs/cosmo_functions.py:7-21, ``dDdtoverD``): dD/dz over dt/dz over D.
+
+    The reference takes forward differences (step 1e-10) of cosmolopy's growth factor and of the
+    age of the universe; here dD/dz is a central difference of the Carroll-Press-Turner D(z) and
+    dt/dz = -1 / ((1 + z) H(z)) is exact."""
+    dlnd_dz = (growth_factor(z + dz, cosmo) - growth_factor(z - dz, cosmo)) / (2.0 * dz) / growth_factor(z, cosmo)
+    return -dlnd_dz * (1.0 + z) * hubble(z, cosmo)
 
 
 def virial_mass(t_vir: float, z: float, cosmo: Cosmology, mu: float | None = None) -> float:

@@ -101,9 +101,18 @@ class InitialConditions:
         S = self.plan.fft_c2r(self.shaped(H, -1, filter_type, ref_compat))
         out["smoothed"] = self.subsample(S, self.norm)
         del S
+        out.update(self.velocities(H, self.norm, filter_type, ref_compat))
+        return out
+
+    def velocities(self, H: torch.Tensor, scale: float, filter_type: int = 0, ref_compat: bool = False,
+                   pixel_factor=None) -> dict:
+        """{"vx", "vy", "vz"}: scale * IFFT(W(kR) i k_c / k^2 H) subsampled onto HII_DIM^3, the
+        inverse FFT unnormalised (set_velocity, HII_filter and subsample: initialize.cu:12-40,
+        133-190; perturb_field.cu:39-88)."""
+        out = {}
         for c, name in enumerate(("vx", "vy", "vz")):
             V = self.plan.fft_c2r(self.shaped(H, c, filter_type, ref_compat))
-            out[name] = self.subsample(V, self.norm)
+            out[name] = self.subsample(V, scale, pixel_factor=pixel_factor)
             del V
         return out
 

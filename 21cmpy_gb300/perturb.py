@@ -4,6 +4,8 @@ excursion-set input boxes (21cmpy's Programs/perturb_field.py:39-128, perturb_fi
 ``PerturbPlan`` owns the device tables and the fixed-point accumulator of one (DIM, HII_DIM) pair;
 its ``move_mass`` runs ``pf_move_mass`` (integer atomics, so the result does not depend on the
 order in which the scattered masses land).  ``evolve_linear`` runs ``pf_evolve_linear``.
+``updated_velocities`` recomputes the velocity boxes at the evolved redshift
+(perturb_field.py:110-125) with the engine's real FFTs and the initial-conditions k-space kernels.
 """
 from __future__ import annotations
 
@@ -94,3 +96,17 @@ def evolve_linear(delta: torch.Tensor, growth: float, out=None, stream=None) -> 
                               _stream(delta.device, stream))
     _lib.check("pf_evolve_linear", rc, lib)
     return out
+
+
+def updated_velocities(deltax: torch.Tensor, hii_dim: int, box_len: float, growth_rate: float,
+                       pixel_factor: float | None = None, filter_type: int = 0, ref_compat: bool = False) -> dict:
+    """Velocity boxes of the DIM^3 density ``deltax`` (perturb_field.py:110-125): per component c,
+    (dD/dt / D) IFFT(W(kR) i k_c / k^2 FFT(deltax)) with a normalised inverse, R = L_FACTOR *
+    BOX_LEN / HII_DIM, subsampled onto HII_DIM^3 (nearest cell).  Returns {"vx", "vy", "vz"}."""
+    from .initial import InitialConditions
+    dim = int(deltax.shape[0])
+    _check_f32(deltax, (dim,) * 3, "deltax", deltax.device)
+    with InitialConditions(dim, hii_dim, box_len, device=deltax.device) as ic:
+        H = ic.plan.fft_r2c(deltax)
+        scale = float(np.float32(growth_rate)) / float(dim) ** 3
+        return ic.velocities(H, scale, filter_type, ref_compat, pixel_factor=pixel_factor)

@@ -435,6 +435,18 @@ def run_perturb(dev, hbm_gbs: float, reps: int = 20):
             e1.synchronize()
             total += e0.elapsed_time(e1)
     ms = total / reps
+    # the velocity boxes at z = 8 from the same density (one 512^3 forward FFT, three inverse ones)
+    ini = importlib.import_module("21cmpy_gb300.initial")
+    scale = float(np.float32(cos.growth_rate(8.0, cos.PLANCK13))) / dim ** 3
+    with ini.InitialConditions(dim, sw, 128.0, device=dev) as ic:
+        for _ in range(2):
+            ic.velocities(ic.plan.fft_r2c(d), scale)
+        e0.record()
+        for _ in range(5):
+            ic.velocities(ic.plan.fft_r2c(d), scale)
+        e1.record()
+        e1.synchronize()
+    vel_ms = e0.elapsed_time(e1) / 5
     # the oracle (float32 numpy restatement, one thread) on the first 64 DIM planes of the same input
     po = importlib.import_module("oracle.pf_oracle")
     dh = d[:64].cpu().numpy()
@@ -452,6 +464,9 @@ def run_perturb(dev, hbm_gbs: float, reps: int = 20):
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_gbs, "unit": "GB/s", "frac": gbs / hbm_gbs,
                          "bytes_model": "4 B / DIM cell + 40 B / HII cell"},
             "l2": "flushed (256 MiB write) before every timed launch",
+            "velocities_ms": vel_ms,
+            "velocities_workload": "updated velocity boxes at z = 8 from the 512^3 density: forward 512^3 FFT, "
+                                   "3 x (k-space shape, inverse 512^3 FFT, subsample to 128^3)",
             "cpu_baseline": {"value": cpu_rate, "unit": "cells/s", "cores": 1, "kind": "port",
                              "sample": f"64 of 512 DIM planes, numpy float32 oracle, one thread, {cpu_s:.1f} s"}}
 

@@ -8,6 +8,11 @@ Only the tests import it.  It restates, with numpy float32 operations in the ref
   v * (D(z) - D(z_init)) / BOX_LEN of the HII cell it lies in (index floor(a / PIXEL_FACTOR)),
   is scaled to the HII grid, wrapped by repeated +- HII_DIM, truncated to a cell index, and adds
   its mass 1 + D(z_init) delta there; the grid is divided by MASS_FACTOR and 1 is subtracted.
+* ``velocities`` -- perturb_field.py:110-125 with set_velocity / filter / subsample
+  (perturb_field.cu:39-88): per component c, (dD/dt / D) irfftn(W(kR) i k_c / k^2 rfftn(deltax)) in
+  float64 (forward unnormalised, inverse normalised, as pyfft), zero at k = 0 and at the
+  component's Nyquist index (the real part of the reference's complex inverse drops it), then the
+  nearest-cell subsample.
 
 The reference sums the masses with float atomics (order-dependent); this restatement sums each
 cell's float32 mass as a 64-bit fixed-point integer with 32 fraction bits (round half to even),
@@ -92,3 +97,25 @@ def move_mass(deltax, vx, vy, vz, init_growth: float, disp_scale: float, pixel_f
     out = ((m / np.float32(mass_factor)).astype(np.float32) - np.float32(1)).astype(np.float32)
     out = out.reshape(sw, sw, sw)
     return (out, sums.reshape(sw, sw, sw)) if return_sums else out
+
+
+def velocities(deltax, hii_dim: int, box_len: float, R: float, growth_rate: float, pixel_factor: float,
+               filter_type: int = 0, ref_compat: bool = False) -> dict:
+    """Float64 velocity boxes at the evolved redshift from the DIM^3 density (perturb_field.py:110-125)."""
+    from oracle import es_oracle, ic_oracle
+    d = np.asarray(deltax, np.float64)
+    n = d.shape[0]
+    L = float(np.float32(box_len))
+    dk = float(np.float32(2.0 * np.pi / L))
+    m = np.fft.fftfreq(n, d=1.0 / n).astype(np.int64)
+    mz = np.arange(n // 2 + 1)
+    k2 = m[:, None, None] ** 2 + m[None, :, None] ** 2 + mz[None, None, :] ** 2
+    X = np.fft.rfftn(d) * es_oracle.window(k2, dk, R, filter_type, ref_compat)
+    ks2 = np.where(k2 == 0, 1, k2) * dk * dk
+    comps = (m[:, None, None] * dk, m[None, :, None] * dk, mz[None, None, :] * dk)
+    nyq = (m[:, None, None] == -n // 2, m[None, :, None] == -n // 2, mz[None, None, :] == n // 2)
+    out = {}
+    for c, name in enumerate(("vx", "vy", "vz")):
+        f = np.where((k2 == 0) | nyq[c], 0.0, comps[c] / ks2) * float(np.float32(growth_rate))
+        out[name] = ic_oracle.subsample(np.fft.irfftn(1j * f * X, s=(n, n, n), axes=(0, 1, 2)), hii_dim, pixel_factor)
+    return out

@@ -69,6 +69,25 @@ def test_move_mass_full_size_conserves_mass(pt):
     assert torch.isfinite(a).all()
 
 
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("dim,sw,ref_compat", [(64, 32, False), (128, 64, True), (256, 128, False)])
+def test_velocities_match_float64_restatement(pt, dim, sw, ref_compat):
+    L = 1.5 * dim
+    rng = np.random.default_rng(dim)
+    delta = (rng.standard_normal((dim,) * 3) * 1.5).astype(np.float32)
+    rate = np.float32(cos.growth_rate(9.0, cos.PLANCK13))
+    pf = np.float32(dim) / np.float32(sw)
+    R = float(np.float32(np.float32(0.620350491) * np.float32(L) / np.float32(sw)))
+    got = pt.updated_velocities(torch.from_numpy(delta).cuda(), sw, L, float(rate), pixel_factor=float(pf),
+                                ref_compat=ref_compat)
+    ref = PO.velocities(delta, sw, L, R, rate, pf, ref_compat=ref_compat)
+    for name in ("vx", "vy", "vz"):
+        assert _rel(got[name].cpu().numpy(), ref[name]) < 2e-5, name
+
+
 def test_evolve_linear_is_bit_exact(pt):
     rng = np.random.default_rng(7)
     x = rng.standard_normal((64,) * 3).astype(np.float32)
@@ -95,6 +114,14 @@ def test_drop_in_program_reads_and_writes_reference_files(pt, tmp_path):
     fg0 = np.float32(cos.growth_factor(300.0, cos.PLANCK13))
     ref = PO.move_mass(delta, *v, fg0, np.float32((fg - fg0) / np.float32(L)), 2.0, 8.0)
     assert np.array_equal(out, ref)
+    # the velocity boxes at z = 8 (perturb_field.py:110-125)
+    rate = np.float32(cos.growth_rate(8.0, cos.PLANCK13))
+    R = float(np.float32(np.float32(0.620350491) * np.float32(L) / np.float32(sw)))
+    vref = PO.velocities(delta, sw, L, R, rate, 2.0)
+    for c in "xyz":
+        got = np.load(boxes / f"updated_v{c}overddot_32_100Mpc.npy")
+        assert got.dtype == np.float32 and got.shape == (sw,) * 3
+        assert _rel(got, vref["v" + c]) < 2e-5, c
     np.save(boxes / "smoothed_deltax_z0.00_32_100Mpc.npy", delta[:32, :32, :32].copy())
     lin = prog.run(8.0, params=params, linear=True)
     assert np.array_equal(lin, PO.evolve_linear(delta[:32, :32, :32], fg))

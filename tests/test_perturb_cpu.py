@@ -74,3 +74,43 @@ def test_linear_evolution_and_file_names():
     assert pf.output_name(12.0, p) == "updated_smoothed_deltax_z12.00_128_300Mpc"
     g = pf.growth(0.0, module("Programs._common").params())
     assert g == np.float32(1.0)
+
+
+def test_growth_rate_limits():
+    cos = module("cosmology")
+    P = cos.PLANCK13
+    # matter domination: D grows as a, so (dD/dt) / D = H(z)
+    assert abs(cos.growth_rate(50.0, P) / cos.hubble(50.0, P) - 1.0) < 1e-4
+    # today: f = dlnD/dlna near Om^0.55 (Linder 2005), within the Carroll-Press-Turner fit
+    f0 = cos.growth_rate(0.0, P) / cos.hubble(0.0, P)
+    assert abs(f0 / P.omega_M_0 ** 0.55 - 1.0) < 0.04
+    # H0 = 100 h km/s/Mpc in 1/s
+    assert abs(cos.hubble(0.0, P) / (P.h * 3.2407792894e-18) - 1.0) < 1e-9
+
+
+def test_velocity_divergence_is_minus_rate_times_smoothed_density():
+    # with nearest-cell subsampling at pixel factor 1, div v = -(dD/dt / D) delta_smoothed on every
+    # non-zero mode except the Nyquist planes, whose derivative the velocity boxes drop
+    from oracle import es_oracle
+    n, L, R, rate = 32, 64.0, 1.5, 2.0
+    rng = np.random.default_rng(4)
+    d = rng.standard_normal((n,) * 3)
+    v = PO.velocities(d, n, L, R, rate, 1.0)
+    dk = float(np.float32(2 * np.pi / L))
+    m = np.fft.fftfreq(n, d=1.0 / n)
+    mz = np.arange(n // 2 + 1)
+    k2 = (m[:, None, None] ** 2 + m[None, :, None] ** 2 + mz[None, None, :] ** 2).astype(np.int64)
+    div = (1j * dk * m[:, None, None] * np.fft.rfftn(v["vx"]) + 1j * dk * m[None, :, None] * np.fft.rfftn(v["vy"])
+           + 1j * dk * mz[None, None, :] * np.fft.rfftn(v["vz"]))
+    smooth = np.fft.rfftn(d) * es_oracle.window(k2, dk, R, 0, False)
+    keep = (np.abs(m[:, None, None]) < n // 2) & (np.abs(m[None, :, None]) < n // 2) & (mz[None, None, :] < n // 2)
+    keep = np.broadcast_to(keep, div.shape) & (k2 > 0)          # the mean has no velocity
+    err = np.abs(div + float(np.float32(rate)) * smooth)[keep].max()
+    assert err < 1e-9 * np.abs(smooth).max()
+    assert all(x.shape == (n,) * 3 for x in v.values())
+
+
+def test_velocity_file_names():
+    pf = module("Programs.perturb_field")
+    p = {"HII_DIM": 128, "BOX_LEN": 300.0}
+    assert pf.velocity_name("x", p) == "updated_vxoverddot_128_300Mpc"
