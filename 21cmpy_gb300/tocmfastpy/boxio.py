@@ -1,4 +1,4 @@
-"""21cmFAST box file names and raw boxes (tocmfastpy/boxio.py:30-253, Programs/IO_utils.py:18-26).
+"""21cmFAST box file names and raw boxes (tocmfastpy/boxio.py:30-293, Programs/IO_utils.py:18-26).
 
 The file name carries the box parameters (``_z``, ``_nf``, ``_eff``, ``_HIIfilter``,
 ``_RHIImax``, ``_<HIIdim>_<L>Mpc``, ``_L``); raw boxes are float32 C-order, optionally with
@@ -26,6 +26,13 @@ class Box:
         self.dim = self.param_dict.get("dim")
         self.z = self.param_dict.get("z", -1)
         self.init = box_data is not None
+
+    def setBox(self, box_data, param_dict):  # noqa: N802 (the reference's name, Box.py:24-31)
+        self.box_data = box_data
+        self.param_dict = param_dict
+        self.dim = param_dict["dim"]
+        self.z = param_dict["z"]
+        self.init = True
 
 
 _TYPES = [("updated_smoothed_deltax", "density"), ("xH_nohalos", "xh"), ("delta_T", "deltaT"),
@@ -109,9 +116,12 @@ def open_box(filename: str, dim: int) -> np.ndarray:
     return trim_box(data.reshape(shape))
 
 
-def readbox(filename: str, quiet: bool = True) -> Box:
-    """Read a 21cmFAST box and its file-name parameters (boxio.py:30-49)."""
+def readbox(filename: str, quiet: bool = False) -> Box:
+    """Read a 21cmFAST box and its file-name parameters (boxio.py:30-49); prints the parameters
+    unless quiet, as the reference does."""
     d = parse_filename(filename)
+    if not quiet:
+        print(d)
     if "HIIdim" not in d:
         raise BoxFormatError(f"{filename}: no _<dim>_<L>Mpc field in the file name")
     return Box(open_box(filename, d["HIIdim"]), d)
@@ -119,6 +129,21 @@ def readbox(filename: str, quiet: bool = True) -> Box:
 
 def save_box(filename: str, box: np.ndarray) -> None:
     np.asarray(box, dtype=np.float32).tofile(filename)
+
+
+def find_run_boxes(filename: str) -> list:
+    """Every file of the run that ``filename`` belongs to (boxio.py:272-293): the files in its
+    directory whose names start with its leading alphanumeric tag and carry its
+    ``_<HIIdim>_<BoxSize>Mpc`` field, sorted by name."""
+    d = parse_filename(filename)
+    base, fname = os.path.split(filename)
+    if "HIIdim" not in d:
+        raise BoxFormatError(f"{filename}: no _<dim>_<L>Mpc field in the file name")
+    m = re.match(r"[a-zA-Z0-9]+", fname)
+    if not m:
+        raise BoxFormatError(f"{filename}: the file name has no leading tag")
+    tag, field = m.group(), "_{0}_{1}Mpc".format(d["HIIdim"], d["BoxSize"])
+    return sorted(os.path.join(base, f) for f in os.listdir(base or ".") if f.startswith(tag) and field in f)
 
 
 def find_files(directory: str, pattern: str = "*") -> np.ndarray:

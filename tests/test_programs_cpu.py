@@ -77,3 +77,22 @@ def test_engine_calls_need_a_gpu():
     with pytest.raises(Exception):
         fhb.conv_bubbles(np.zeros((32, 32, 32), np.float32), {"BoxSize": 48, "HIIdim": 32, "z": 8.0},
                          fil=0, quiet=True, params={"ZETA": 30.0})
+
+
+def test_run_boxes_and_box_fields(tmp_path, capsys):
+    names = ["xH_nohalos_z8.00_nf0.5_eff30.0_8_20Mpc", "xH_nohalos_z9.00_nf0.7_eff30.0_8_20Mpc",
+             "xH_nohalos_z9.00_nf0.7_eff30.0_16_20Mpc", "delta_T_z8.00_8_20Mpc"]
+    for n in names:
+        np.zeros((8, 8, 8), np.float32).tofile(tmp_path / n)
+    run = boxio.find_run_boxes(str(tmp_path / names[1]))
+    assert [os.path.basename(f) for f in run] == sorted(names[:2])
+    b = boxio.readbox(str(tmp_path / names[0]))
+    assert "'nf': 0.5" in capsys.readouterr().out          # the reference prints the parameters
+    assert b.dim == 8 and b.z == 8.0 and b.init and b.box_data.shape == (8, 8, 8)
+    boxio.readbox(str(tmp_path / names[0]), quiet=True)
+    assert capsys.readouterr().out == ""
+    c = boxio.Box()
+    c.setBox(b.box_data, b.param_dict)
+    assert c.init and c.dim == 8
+    with pytest.raises(boxio.BoxFormatError):
+        boxio.find_run_boxes(str(tmp_path / "no_size_field"))
