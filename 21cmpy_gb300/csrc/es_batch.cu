@@ -180,23 +180,23 @@ __device__ __noinline__ void b_row_r2c(const BoxDev& b, int tile, float2* sm) {
   }
   __syncthreads();
   float2* Z = fft_lines<M, false, RL, BT, true, ES, 1, N>(A, B, tw);
-  for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += BT) {
-    const int m = q % (M / 2 + 1), l = q / (M / 2 + 1);
+  // item t of row l makes X[t] and X[M-t] (item 0: the packed (X[0], X[N/2]) and X[M/2])
+  for (int q = threadIdx.x; q < RL * (M / 2); q += BT) {
+    const int t = q % (M / 2), l = q / (M / 2);
     float2* out = b.X + pair0 + (size_t)l * M;
-    if (m == 0) {
+    if (t == 0) {
       const float2 z0 = Z[l];
       out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+      const float2 zh = Z[(M / 2) * ES + l];
+      const float2 th = cmul(tw[M / 2], make_float2(0.f, zh.y + zh.y));
+      out[M / 2] = make_float2(0.5f * (zh.x + zh.x + th.y), -0.5f * th.x);
     } else {
-      const int m2 = M - m;
-      const float2 zm = Z[m * ES + l], zc = Z[m2 * ES + l];
-      {
-        const float2 t = cmul(tw[m], make_float2(zm.x - zc.x, zm.y + zc.y));
-        out[m] = make_float2(0.5f * (zm.x + zc.x + t.y), 0.5f * (zm.y - zc.y - t.x));
-      }
-      if (m2 != m) {
-        const float2 t = cmul(tw[m2], make_float2(zc.x - zm.x, zc.y + zm.y));
-        out[m2] = make_float2(0.5f * (zc.x + zm.x + t.y), 0.5f * (zc.y - zm.y - t.x));
-      }
+      const int m2 = M - t;
+      const float2 zm = Z[t * ES + l], zc = Z[m2 * ES + l], w = tw[t];
+      const float2 t1 = cmul(w, make_float2(zm.x - zc.x, zm.y + zc.y));
+      out[t] = make_float2(0.5f * (zm.x + zc.x + t1.y), 0.5f * (zm.y - zc.y - t1.x));
+      const float2 t2 = cmul(make_float2(-w.x, w.y), make_float2(zc.x - zm.x, zc.y + zm.y));   // w^(M-t)
+      out[m2] = make_float2(0.5f * (zc.x + zm.x + t2.y), 0.5f * (zc.y - zm.y - t2.x));
     }
   }
 }
@@ -211,21 +211,22 @@ __device__ __noinline__ void b_row_c2r(const BoxDev& b, int radius, int tile, fl
   __syncthreads();                                        // the split below reads the twiddles
   const size_t pair0 = (size_t)tile * RL * M;
   const float2* src = b.T + pair0;
-  for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += BT) {
-    const int m = q % (M / 2 + 1), l = q / (M / 2 + 1);
+  // item t of row l makes Z[t] and Z[M-t] (item 0: Z[0] from (X[0], X[N/2]) and Z[M/2])
+  for (int q = threadIdx.x; q < RL * (M / 2); q += BT) {
+    const int t = q % (M / 2), l = q / (M / 2);
     const float2* x = src + (size_t)l * M;
-    if (m == 0) {
-      const float2 x0 = __ldcg(x);
+    if (t == 0) {
+      const float2 x0 = __ldcg(x), xh = __ldcg(x + M / 2);
       A[l] = make_float2(x0.x + x0.y, x0.x - x0.y);
+      const float2 th = cmul(cconj(tw[M / 2]), make_float2(0.f, xh.y + xh.y));
+      A[(M / 2) * ES + l] = make_float2(xh.x + xh.x - th.y, th.x);
     } else {
-      const int m2 = M - m;
-      const float2 xm = __ldcg(x + m), xc = __ldcg(x + m2);
-      const float2 t1 = cmul(cconj(tw[m]), make_float2(xm.x - xc.x, xm.y + xc.y));
-      A[m * ES + l] = make_float2(xm.x + xc.x - t1.y, xm.y - xc.y + t1.x);
-      if (m2 != m) {
-        const float2 t2 = cmul(cconj(tw[m2]), make_float2(xc.x - xm.x, xc.y + xm.y));
-        A[m2 * ES + l] = make_float2(xc.x + xm.x - t2.y, xc.y - xm.y + t2.x);
-      }
+      const int m2 = M - t;
+      const float2 xm = __ldcg(x + t), xc = __ldcg(x + m2), w = tw[t];
+      const float2 t1 = cmul(cconj(w), make_float2(xm.x - xc.x, xm.y + xc.y));
+      A[t * ES + l] = make_float2(xm.x + xc.x - t1.y, xm.y - xc.y + t1.x);
+      const float2 t2 = cmul(make_float2(-w.x, -w.y), make_float2(xc.x - xm.x, xc.y + xm.y));   // conj w^(M-t)
+      A[m2 * ES + l] = make_float2(xc.x + xm.x - t2.y, xc.y - xm.y + t2.x);
     }
   }
   __syncthreads();

@@ -99,23 +99,27 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
     }
     __syncthreads();
     if (s_abort) break;
-    // C2R split + transpose: Z[m] = (X[m] + conj X[M-m]) + i w^-m (X[m] - conj X[M-m])
+    // C2R split + transpose: Z[m] = (X[m] + conj X[M-m]) + i w^-m (X[m] - conj X[M-m]).  Item t of
+    // row l makes Z[t] and Z[M-t]; item 0 makes Z[0] from the packed (X[0], X[N/2]) and the
+    // self-paired Z[M/2].  RL * M/2 items: every thread has whole items, no division when M/2 is a
+    // power of two.  w^-(M-t) = -w^t, so one twiddle serves both outputs.
     const float2* src = s ? S1 : S0;
-    for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += T) {
-      const int m = q % (M / 2 + 1), l = q / (M / 2 + 1);
+    for (int q = threadIdx.x; q < RL * (M / 2); q += T) {
+      const int t = q % (M / 2), l = q / (M / 2);
       const float2* x = src + l * M;
-      if (m == 0) {
+      if (t == 0) {
         const float2 x0 = x[0];                       // (X[0], X[N/2]), both real
         A[l] = make_float2(x0.x + x0.y, x0.x - x0.y);
+        const float2 xh = x[M / 2];
+        const float2 th = cmul(cconj(tw[M / 2]), make_float2(0.f, xh.y + xh.y));
+        A[(M / 2) * ES + l] = make_float2(xh.x + xh.x - th.y, th.x);
       } else {
-        const int m2 = M - m;
-        const float2 xm = x[m], xc = x[m2];
-        const float2 t1 = cmul(cconj(tw[m]), make_float2(xm.x - xc.x, xm.y + xc.y));
-        A[m * ES + l] = make_float2(xm.x + xc.x - t1.y, xm.y - xc.y + t1.x);
-        if (m2 != m) {
-          const float2 t2 = cmul(cconj(tw[m2]), make_float2(xc.x - xm.x, xc.y + xm.y));
-          A[m2 * ES + l] = make_float2(xc.x + xm.x - t2.y, xc.y - xm.y + t2.x);
-        }
+        const int m2 = M - t;
+        const float2 xm = x[t], xc = x[m2], w = tw[t];
+        const float2 t1 = cmul(cconj(w), make_float2(xm.x - xc.x, xm.y + xc.y));
+        A[t * ES + l] = make_float2(xm.x + xc.x - t1.y, xm.y - xc.y + t1.x);
+        const float2 t2 = cmul(make_float2(-w.x, -w.y), make_float2(xc.x - xm.x, xc.y + xm.y));
+        A[m2 * ES + l] = make_float2(xc.x + xm.x - t2.y, xc.y - xm.y + t2.x);
       }
     }
     if (a.discard_in) {
@@ -239,24 +243,24 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_r2
     }
     __syncthreads();
     float2* Z = fft_lines<M, false, RL, T, true, ES, 1, N>(A, B, tw);
-    // X[m] = (Z[m] + conj Z[M-m]) / 2 - i w^m (Z[m] - conj Z[M-m]) / 2
-    for (int q = threadIdx.x; q < RL * (M / 2 + 1); q += T) {
-      const int m = q % (M / 2 + 1), l = q / (M / 2 + 1);
+    // X[m] = (Z[m] + conj Z[M-m]) / 2 - i w^m (Z[m] - conj Z[M-m]) / 2; item t of row l makes X[t]
+    // and X[M-t], item 0 the packed (X[0], X[N/2]) and the self-paired X[M/2]; w^(M-t) = -conj w^t
+    for (int q = threadIdx.x; q < RL * (M / 2); q += T) {
+      const int t = q % (M / 2), l = q / (M / 2);
       float2* out = a.cout + pair0 + (size_t)l * M;
-      if (m == 0) {
+      if (t == 0) {
         const float2 z0 = Z[l];
         out[0] = make_float2(z0.x + z0.y, z0.x - z0.y);
+        const float2 zh = Z[(M / 2) * ES + l];
+        const float2 th = cmul(tw[M / 2], make_float2(0.f, zh.y + zh.y));
+        out[M / 2] = make_float2(0.5f * (zh.x + zh.x + th.y), -0.5f * th.x);
       } else {
-        const int m2 = M - m;
-        const float2 zm = Z[m * ES + l], zc = Z[m2 * ES + l];
-        {
-          const float2 t = cmul(tw[m], make_float2(zm.x - zc.x, zm.y + zc.y));
-          out[m] = make_float2(0.5f * (zm.x + zc.x + t.y), 0.5f * (zm.y - zc.y - t.x));
-        }
-        if (m2 != m) {
-          const float2 t = cmul(tw[m2], make_float2(zc.x - zm.x, zc.y + zm.y));
-          out[m2] = make_float2(0.5f * (zc.x + zm.x + t.y), 0.5f * (zc.y - zm.y - t.x));
-        }
+        const int m2 = M - t;
+        const float2 zm = Z[t * ES + l], zc = Z[m2 * ES + l], w = tw[t];
+        const float2 t1 = cmul(w, make_float2(zm.x - zc.x, zm.y + zc.y));
+        out[t] = make_float2(0.5f * (zm.x + zc.x + t1.y), 0.5f * (zm.y - zc.y - t1.x));
+        const float2 t2 = cmul(make_float2(-w.x, w.y), make_float2(zc.x - zm.x, zc.y + zm.y));
+        out[m2] = make_float2(0.5f * (zc.x + zm.x + t2.y), 0.5f * (zc.y - zm.y - t2.x));
       }
     }
     __syncthreads();
