@@ -25,6 +25,9 @@ OPT_ROW_TILE = 3
 OPT_L2_HINTS = 4
 OPT_COL_RADIX = 5
 OPT_ROW_RADIX = 6
+OPT_OVERLAP = 7
+OPT_ROW_CTAS = 8
+OPT_COL_CTAS = 9
 
 
 class EngineUnavailable(RuntimeError):

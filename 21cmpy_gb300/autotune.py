@@ -4,7 +4,9 @@ For a box size it times, on the device, every combination of the TMA passes' til
 (``ES_OPT_COL_TILE`` x ``ES_OPT_ROW_TILE``) and of the per-radius passes' radix schedules
 (``ES_OPT_COL_RADIX`` x ``ES_OPT_ROW_RADIX``: radices up to 16, or up to 8 with one more stage),
 plus the synchronous-tile passes, running one whole box through the path (forward transform,
-every radius, final step, delta_T and P(k)), and keeps the fastest.  Results are cached per GPU model, box size and library version in a JSON file
+every radius, final step, delta_T and P(k)), and keeps the fastest.  A second stage times, on the
+best of those, the overlapped-radius schedules (``ES_OPT_OVERLAP`` with per-SM CTA caps
+``ES_OPT_ROW_CTAS`` / ``ES_OPT_COL_CTAS``), then the runner-up tile shapes with the best schedule.  Results are cached per GPU model, box size and library version in a JSON file
 (``$ES_AUTOTUNE_CACHE`` or ``~/.cache/21cmpy_gb300/autotune.json``), so later plans of the same
 size start tuned.
 """
@@ -23,6 +25,12 @@ from . import _lib, cosmology, schedule
 # (variant, col tile, row tile, col radix schedule, row radix schedule)
 CANDIDATES = [(1, c, r, cr, rr) for c in range(3) for r in range(4) for cr in range(2) for rr in range(2)] + \
     [(0, 0, 0, 0, 0)]
+# (overlap, row-pass CTAs per SM, column-pass CTAs per SM), appended to a tile configuration
+OVERLAP = [(0, 0, 0), (1, 0, 0), (1, 1, 1), (1, 1, 2), (1, 1, 3), (1, 2, 1), (1, 2, 2)]
+
+
+def with_overlap(config, ov) -> tuple:
+    return tuple(config)[:5] + tuple(ov)
 _lock = threading.Lock()
 
 
@@ -55,13 +63,16 @@ def _store(table: dict):
 
 
 def apply(plan, config) -> None:
-    config = tuple(config) + (0, 0)[: max(0, 5 - len(config))]    # entries without radix schedules
-    variant, col_tile, row_tile, col_radix, row_radix = config[:5]
+    config = tuple(config) + (0,) * max(0, 8 - len(config))    # entries without later options
+    variant, col_tile, row_tile, col_radix, row_radix, overlap, row_ctas, col_ctas = config[:8]
     plan.set_option(_lib.OPT_COL_VARIANT, variant)
     plan.set_option(_lib.OPT_COL_TILE, col_tile)
     plan.set_option(_lib.OPT_ROW_TILE, row_tile)
     plan.set_option(_lib.OPT_COL_RADIX, col_radix)
     plan.set_option(_lib.OPT_ROW_RADIX, row_radix)
+    plan.set_option(_lib.OPT_OVERLAP, overlap)
+    plan.set_option(_lib.OPT_ROW_CTAS, row_ctas)
+    plan.set_option(_lib.OPT_COL_CTAS, col_ctas)
 
 
 def cached(device, n: int):
@@ -86,14 +97,14 @@ def tune(plan, repeats: int = 3, store: bool = True) -> dict:
         dT = torch.empty_like(d)
         stream = torch.cuda.current_stream(dev)
         times = {}
-        for cfg in CANDIDATES:
+
+        def box():
+            plan.run(d, st, out=xh)
+            _, ave = plan.delta_T(xh, d, c, out=dT)
+            plan.power_spectrum(dT, ave, edges)
+
+        def time_config(cfg):
             apply(plan, cfg)
-
-            def box():
-                plan.run(d, st, out=xh)
-                _, ave = plan.delta_T(xh, d, c, out=dT)
-                plan.power_spectrum(dT, ave, edges)
-
             box()
             torch.cuda.synchronize(dev)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -102,7 +113,17 @@ def tune(plan, repeats: int = 3, store: bool = True) -> dict:
                 box()
             e1.record(stream)
             e1.synchronize()
-            times[cfg] = e0.elapsed_time(e1) / repeats
+            times[tuple(cfg)] = e0.elapsed_time(e1) / repeats
+
+        for cfg in CANDIDATES:
+            time_config(with_overlap(cfg, OVERLAP[0]))
+        ranked = sorted(times, key=times.get)
+        for ov in OVERLAP[1:]:
+            time_config(with_overlap(ranked[0], ov))
+        best_ov = min(times, key=times.get)[5:]
+        for cfg in ranked[1:3]:
+            if with_overlap(cfg, best_ov) not in times:
+                time_config(with_overlap(cfg, best_ov))
         plan.check()
         best = min(times, key=times.get)
         apply(plan, best)

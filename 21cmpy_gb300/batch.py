@@ -116,6 +116,110 @@ class BatchedExcursionSet:
         self.close()
 
 
+class PlanGraphBatch:
+    """x_HI of many boxes through per-box plans on concurrent streams, captured once into a CUDA
+    graph and replayed.
+
+    Boxes are grouped by (HII_DIM, BOX_LEN); each group gets up to ``lanes`` plans, each with its own
+    stream, and a lane runs its boxes (forward transform, radius loop, final step) one after the
+    other while the lanes of all groups run side by side.  The plans use the TMA passes, whose
+    radius parameters are kernel arguments, so a whole batch is a static graph; ``tune`` applies
+    the autotuner's configuration of every box size (overlapped radii included).
+    """
+
+    def __init__(self, boxes, output: str = "xH", lanes: int = 2, use_graph: bool = True, tune: bool = True,
+                 device=None):
+        from .autotune import ensure_tuned
+        from .engine import ExcursionSetPlan
+        if not torch.cuda.is_available():
+            raise _lib.EngineUnavailable("the batched engine needs a CUDA device")
+        if lanes < 1:
+            raise ValueError("lanes must be >= 1")
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.output = output
+        self.inputs, self.setups = [], []
+        for d, st in boxes:
+            if not isinstance(d, torch.Tensor) or d.device != self.device or d.dtype != torch.float32:
+                raise ValueError("densities must be float32 tensors on the batch's device")
+            self.inputs.append(d)
+            self.setups.append(st)
+        if not self.setups:
+            raise ValueError("empty batch")
+        self.out = [torch.empty_like(d) for d in self.inputs]
+        self.nf = torch.zeros(len(self.setups), dtype=torch.float32, device=self.device)
+        groups: dict = {}
+        for i, st in enumerate(self.setups):
+            groups.setdefault((st.n, float(st.box_len)), []).append(i)
+        self.lanes = []                       # (plan, stream, [box indices])
+        with torch.cuda.device(self.device):
+            for (n, L), idx in sorted(groups.items()):
+                k = min(lanes, len(idx))
+                radii = max(self.setups[i].n_radii for i in idx)
+                for j in range(k):
+                    plan = ExcursionSetPlan(n, L, max_radii=max(64, radii), device=self.device)
+                    if tune:
+                        ensure_tuned(plan)
+                    if plan.col_variant != 1:
+                        plan.col_variant = 1           # graph capture needs the TMA passes
+                    self.lanes.append((plan, torch.cuda.Stream(self.device), idx[j::k]))
+        self.use_graph = bool(use_graph)
+        self.graph = None
+
+    def _body(self):
+        cur = torch.cuda.current_stream(self.device)
+        fork = torch.cuda.Event()
+        fork.record(cur)
+        for _plan, s, _idx in self.lanes:
+            s.wait_event(fork)
+        longest = max(len(idx) for _p, _s, idx in self.lanes)
+        for step in range(longest):                    # hand every lane its next box in turn
+            for plan, s, idx in self.lanes:
+                if step < len(idx):
+                    i = idx[step]
+                    plan.run(self.inputs[i], self.setups[i], out=self.out[i], nf=self.nf[i:i + 1],
+                             output=self.output, stream=s)
+        for _plan, s, _idx in self.lanes:
+            cur.wait_stream(s)
+
+    def run(self, stream=None):
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.device(self.device), torch.cuda.stream(s):
+            if not self.use_graph:
+                self._body()
+            else:
+                if self.graph is None:
+                    self._body()                       # warm-up outside the capture
+                    torch.cuda.synchronize(self.device)
+                    self.graph = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(self.graph):
+                        self._body()
+                self.graph.replay()
+        return self.out, self.nf
+
+    def check(self, stream=None):
+        for plan, _s, _idx in self.lanes:
+            plan.check(stream)
+
+    def voxel_radius_updates(self) -> int:
+        return sum(st.n ** 3 * st.n_radii for st in self.setups)
+
+    def info(self) -> dict:
+        return {"lanes": len(self.lanes), "boxes": len(self.setups),
+                "plans": sorted({(p.n, len(idx)) for p, _s, idx in self.lanes})}
+
+    def close(self):
+        self.graph = None
+        for plan, _s, _idx in getattr(self, "lanes", []):
+            plan.close()
+        self.lanes = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 def boxes_from_specs(specs, device=None, cosmo=None, table=None):
     """(device density, IonizeSetup) pairs for BoxSpec entries (seeded GRF at each box's z)."""
     from .cosmology import BASELINE_COSMO

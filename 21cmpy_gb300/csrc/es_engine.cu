@@ -9,6 +9,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "es_engine.h"
@@ -95,6 +96,7 @@ struct es_plan {
   // pinned host staging for per-call parameter uploads
   RadDev* h_rad = nullptr;
   int* h_thr = nullptr;
+  std::vector<RadDev> hr;           // this call's per-radius parameters (kernel arguments by value)
   cudaEvent_t staged = nullptr;     // last upload from the staging buffers
   size_t partial_floats = 0;
   // optional per-launch timing: event pairs around every kernel while enabled
@@ -104,6 +106,15 @@ struct es_plan {
   int prof_dropped = 0;
   // TMA descriptors: main arrays with z-pass and y-pass boxes, Nyquist planes with z-pass boxes
   CUtensorMap tmX_z, tmX_y, tmXn, tmT_z, tmT_y, tmTn;
+  // overlapped radii: a second intermediate spectrum so the column passes of radius r + 1 run on
+  // the plan's own stream while the row pass of radius r runs on the caller's
+  float2* T2 = nullptr;
+  float2* Tnyq2 = nullptr;
+  CUtensorMap tmT2_z, tmT2_y, tmT2n;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_col[2] = {nullptr, nullptr}, ev_row[2] = {nullptr, nullptr};
+  int overlap = 0;                  // ES_OPT_OVERLAP
+  int row_per_sm = 0, col_per_sm = 0;   // ES_OPT_ROW_CTAS / ES_OPT_COL_CTAS caps (0 = by occupancy)
   int col_variant = 1;              // passes: 1 TMA double-buffered (default), 0 synchronous
   int col_tile = 0, row_tile = 0;   // TMA tile-shape variants
   int col_radix = 0, row_radix = 0; // radix schedules of the per-radius passes
@@ -119,7 +130,7 @@ constexpr int kStatsStride = 4;
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
-  size_t X, Xnyq, T, Tnyq, tw, dR0, dR1, flags, centers, wtab, partials, counters, stats, rad, thr, total;
+  size_t X, Xnyq, T, Tnyq, T2, Tnyq2, tw, dR0, dR1, flags, centers, wtab, partials, counters, stats, rad, thr, total;
 };
 
 Layout layout(int n, int max_radii, size_t partial_floats) {
@@ -132,6 +143,8 @@ Layout layout(int n, int max_radii, size_t partial_floats) {
   L.Xnyq = take(N * N * 8);
   L.T = take(N * N * M * 8);
   L.Tnyq = take(N * N * 8);
+  L.T2 = take(N * N * M * 8);
+  L.Tnyq2 = take(N * N * 8);
   L.tw = take(N * 8);
   L.dR0 = take(N * N * N * 4);
   L.dR1 = take(N * N * N * 4);
@@ -366,7 +379,9 @@ int encode_maps(es_plan* p) {
   const int n = p->n, ti = p->geo.tcol_ti[p->col_tile];
   if ((rc = make_main_map(&p->tmX_z, p->X, n, ti, true)) || (rc = make_main_map(&p->tmX_y, p->X, n, ti, false)) ||
       (rc = make_main_map(&p->tmT_z, p->T, n, ti, true)) || (rc = make_main_map(&p->tmT_y, p->T, n, ti, false)) ||
-      (rc = make_nyq_map(&p->tmXn, p->Xnyq, n, ti)) || (rc = make_nyq_map(&p->tmTn, p->Tnyq, n, ti)))
+      (rc = make_nyq_map(&p->tmXn, p->Xnyq, n, ti)) || (rc = make_nyq_map(&p->tmTn, p->Tnyq, n, ti)) ||
+      (rc = make_main_map(&p->tmT2_z, p->T2, n, ti, true)) || (rc = make_main_map(&p->tmT2_y, p->T2, n, ti, false)) ||
+      (rc = make_nyq_map(&p->tmT2n, p->Tnyq2, n, ti)))
     return rc;
   return ES_OK;
 }
@@ -477,7 +492,7 @@ int forward_into(es_plan* p, const float* in, float scale, bool into_T, cudaStre
 
 extern "C" {
 
-int es_version(void) { return 2; }
+int es_version(void) { return 3; }
 
 int es_last_error(char* buf, int len) {
   if (!buf || len <= 0) return ES_E_ARG;
@@ -532,6 +547,7 @@ int es_plan_create(int n, double box_len, int max_radii, es_plan** out) {
   char* b = static_cast<char*>(p->base);
   p->X = (float2*)(b + L.X); p->Xnyq = (float2*)(b + L.Xnyq);
   p->T = (float2*)(b + L.T); p->Tnyq = (float2*)(b + L.Tnyq);
+  p->T2 = (float2*)(b + L.T2); p->Tnyq2 = (float2*)(b + L.Tnyq2);
   p->tw = (float2*)(b + L.tw);
   p->dR[0] = (float*)(b + L.dR0); p->dR[1] = (float*)(b + L.dR1);
   p->flags = (uint32_t*)(b + L.flags);
@@ -547,8 +563,15 @@ int es_plan_create(int n, double box_len, int max_radii, es_plan** out) {
   if (cudaMallocHost(&p->h_rad, sizeof(RadDev) * max_radii) != cudaSuccess ||
       cudaMallocHost(&p->h_thr, sizeof(int) * es::PK_MAX_BINS) != cudaSuccess)
     return cleanup(fail(ES_E_NOMEM, "es_plan_create: pinned staging allocation failed"));
-  if (cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming) != cudaSuccess)
+  if (cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->ev_col[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->ev_col[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->ev_row[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->ev_row[1], cudaEventDisableTiming) != cudaSuccess)
     return cleanup(fail(ES_E_CUDA, "es_plan_create: cudaEventCreate failed"));
+  if (cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(fail(ES_E_CUDA, "es_plan_create: cudaStreamCreate failed"));
   // twiddles w_n^m = exp(-2 pi i m / n) in double, rounded once
   std::vector<float2> tw(n);
   for (int m = 0; m < n; ++m) {
@@ -568,10 +591,14 @@ int es_plan_destroy(es_plan* p) {
   if (!p) return ES_OK;
   DeviceGuard g(p->device);
   if (p->staged) cudaEventSynchronize(p->staged);
+  if (p->aux) cudaStreamSynchronize(p->aux);
   if (p->base) cudaFree(p->base);
   if (p->h_rad) cudaFreeHost(p->h_rad);
   if (p->h_thr) cudaFreeHost(p->h_thr);
   if (p->staged) cudaEventDestroy(p->staged);
+  for (cudaEvent_t e : {p->ev_fork, p->ev_col[0], p->ev_col[1], p->ev_row[0], p->ev_row[1]})
+    if (e) cudaEventDestroy(e);
+  if (p->aux) cudaStreamDestroy(p->aux);
   for (cudaEvent_t e : p->prof_events) cudaEventDestroy(e);
   delete p;
   return ES_OK;
@@ -596,9 +623,9 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
       return fail(ES_E_ARG, "es_ionize: radius %d has R=%g denom=%g", r, prm->radii[r].R, prm->radii[r].denom);
   DeviceGuard g(p->device);
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = reuse_staging(p);
-  if (rc) return rc;
+  int rc = 0;
   const double scale = p->box_len / p->n;
+  p->hr.resize(nr);
   for (int r = 0; r < nr; ++r) {
     RadDev rd;
     rd.R = prm->radii[r].R;
@@ -623,10 +650,17 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
       while (m >= 0 && (double)m >= rc2) --m;
       rd.r2max = (int)m;
     }
-    p->h_rad[r] = rd;
+    p->hr[r] = rd;
   }
-  ES_CUDA(cudaMemcpyAsync(p->rad, p->h_rad, sizeof(RadDev) * nr, cudaMemcpyHostToDevice, s));
-  ES_CUDA(cudaEventRecord(p->staged, s));
+  // Only the synchronous column pass reads the radii from device memory (its filter tables); the
+  // TMA passes take them as kernel arguments, so with those the call does no host-to-device copy
+  // and no host wait, and can be captured in a CUDA graph.
+  if (p->col_variant == 0) {
+    if ((rc = reuse_staging(p))) return rc;
+    std::copy(p->hr.begin(), p->hr.end(), p->h_rad);
+    ES_CUDA(cudaMemcpyAsync(p->rad, p->h_rad, sizeof(RadDev) * nr, cudaMemcpyHostToDevice, s));
+    ES_CUDA(cudaEventRecord(p->staged, s));
+  }
   const float inv_n3 = (float)(1.0 / ((double)p->n * p->n * p->n));
   int slot = -1;
   if (p->col_variant == 0) {        // the synchronous column pass gathers W from per-radius tables
@@ -646,30 +680,44 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
   const size_t t_bytes = (size_t)p->n * p->n * (p->m + 1) * sizeof(float2);
   const bool keep_T = p->l2_hints && (double)t_bytes <= 0.6 * (double)p->l2_bytes;
   const int keep = keep_T ? es::ES_HINT_EVICT_LAST : es::ES_HINT_NORMAL;
-  for (int r = 0; r < nr; ++r) {
+  // Intermediate spectra: T for every radius, or T / T2 alternating when radii overlap.
+  struct TBuf { float2* main; float2* nyq; const CUtensorMap* mz; const CUtensorMap* my; const CUtensorMap* mn; };
+  const TBuf tb[2] = {{p->T, p->Tnyq, &p->tmT_z, &p->tmT_y, &p->tmTn},
+                      {p->T2, p->Tnyq2, &p->tmT2_z, &p->tmT2_y, &p->tmT2n}};
+  const bool ovl = p->overlap != 0 && nr > 1;
+  auto capped = [&](int grid, int per_sm) { return (ovl && per_sm > 0 && grid > p->sms * per_sm) ? p->sms * per_sm : grid; };
+  const int g_z = capped(grid_col_z(p, false), p->col_per_sm), g_y = capped(grid_col_y(p), p->col_per_sm);
+  const int g_row = capped(grid_row(p, true), p->row_per_sm);
+  // z inverse with the filter of radius r, then y inverse, into the radius' intermediate spectrum
+  auto col_passes = [&](int r, cudaStream_t cs) -> int {
+    const TBuf& t = tb[ovl ? (r & 1) : 0];
     es::OpArgs a = base_args(p);
-    a.cin = p->X; a.cin_nyq = p->Xnyq; a.cout = p->T; a.cout_nyq = p->Tnyq;
+    a.cin = p->X; a.cin_nyq = p->Xnyq; a.cout = t.main; a.cout_nyq = t.nyq;
     a.wtab = p->wtab + (size_t)r * p->k2n;
     a.scale = prm->growth_scale;
-    a.fR = p->h_rad[r].R;
-    a.fk2cut = p->h_rad[r].k2cut;
+    a.fR = p->hr[r].R;
+    a.fk2cut = p->hr[r].k2cut;
     a.filter = prm->filter_type;
     a.ref_compat = prm->ref_compat;
     a.dk = p->dk;
     a.inv_n3 = inv_n3;
     a.hint_in = p->l2_hints ? es::ES_HINT_EVICT_FIRST : es::ES_HINT_NORMAL;
     a.hint_out = keep;
-    set_maps(a, p->tmX_z, p->tmT_z, &p->tmXn, &p->tmTn);
-    if ((rc = run_op(p, es::OP_COL_Z_INV_FILTER, a, grid_col_z(p, false), s))) return rc;
+    set_maps(a, p->tmX_z, *t.mz, &p->tmXn, t.mn);
+    if (int e = run_op(p, es::OP_COL_Z_INV_FILTER, a, g_z, cs)) return e;
     a = base_args(p);
-    a.cin = p->T; a.cin_nyq = p->Tnyq; a.cout = p->T;
+    a.cin = t.main; a.cin_nyq = t.nyq; a.cout = t.main;
     a.hint_in = keep;
     a.hint_out = keep;
-    set_maps(a, p->tmT_y, p->tmT_y, nullptr, nullptr);
-    if ((rc = run_op(p, es::OP_COL_Y_INV, a, grid_col_y(p), s))) return rc;
+    set_maps(a, *t.my, *t.my, nullptr, nullptr);
+    return run_op(p, es::OP_COL_Y_INV, a, g_y, cs);
+  };
+  // x C2R with the excursion-set epilogue of radius r (and the sphere painting of radius r - 1)
+  auto row_pass = [&](int r) -> int {
+    const TBuf& t = tb[ovl ? (r & 1) : 0];
     if (prm->update == 1 && r > 0) ES_CUDA(cudaMemsetAsync(p->counters + 1, 0, sizeof(unsigned), s));
-    a = base_args(p);
-    a.cin = p->T;
+    es::OpArgs a = base_args(p);
+    a.cin = t.main;
     a.rout = reinterpret_cast<float2*>(p->dR[r & 1]);
     a.prev = reinterpret_cast<const float2*>(p->dR[(r + 1) & 1]);
     a.has_prev = r > 0;
@@ -687,13 +735,37 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     a.normalize = prm->normalize_mean;
     a.hint_in = p->l2_hints ? es::ES_HINT_EVICT_FIRST : es::ES_HINT_NORMAL;
     a.discard_in = p->l2_hints;
-    if ((rc = run_op(p, es::OP_ROW_C2R_IONIZE, a, grid_row(p, true), s))) return rc;
+    if (int e = run_op(p, es::OP_ROW_C2R_IONIZE, a, g_row, s)) return e;
     if (prm->update == 1 && r > 0) {
-      slot = prof_begin(p, ES_PROF_PAINT, s);
+      const int ps = prof_begin(p, ES_PROF_PAINT, s);
       paint_kernel<<<p->sms * 4, 256, 0, s>>>(p->centers, p->counters + 1, p->flags, p->n,
-                                              p->h_rad[r - 1].r2max, prm->ref_compat ? 0 : 1);
-      prof_end(p, slot, s);
+                                              p->hr[r - 1].r2max, prm->ref_compat ? 0 : 1);
+      prof_end(p, ps, s);
       ES_CUDA(cudaGetLastError());
+    }
+    return ES_OK;
+  };
+  if (!ovl) {
+    for (int r = 0; r < nr; ++r)
+      if ((rc = col_passes(r, s)) || (rc = row_pass(r))) return rc;
+  } else {
+    // Software pipeline over two streams: the column passes of radius r + 1 (plan stream) run
+    // while the row pass of radius r (caller's stream) runs.  Radius r + 1 writes the spectrum
+    // that radius r - 1 read, so it waits for that row pass; each row pass waits for its own
+    // column passes.  Everything the plan stream does is joined back before the last row pass.
+    ES_CUDA(cudaEventRecord(p->ev_fork, s));
+    ES_CUDA(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
+    if ((rc = col_passes(0, p->aux))) return rc;
+    ES_CUDA(cudaEventRecord(p->ev_col[0], p->aux));
+    for (int r = 0; r < nr; ++r) {
+      if (r + 1 < nr) {
+        if (r >= 1) ES_CUDA(cudaStreamWaitEvent(p->aux, p->ev_row[(r + 1) & 1], 0));
+        if ((rc = col_passes(r + 1, p->aux))) return rc;
+        ES_CUDA(cudaEventRecord(p->ev_col[(r + 1) & 1], p->aux));
+      }
+      ES_CUDA(cudaStreamWaitEvent(s, p->ev_col[r & 1], 0));
+      if ((rc = row_pass(r))) return rc;
+      ES_CUDA(cudaEventRecord(p->ev_row[r & 1], s));
     }
   }
   slot = prof_begin(p, ES_PROF_FINAL, s);
@@ -869,6 +941,15 @@ int es_plan_set_option(es_plan* p, int option, int value) {
       if (value != 0 && value != 1) return fail(ES_E_ARG, "es_plan_set_option: radix schedule must be 0 or 1");
       (option == ES_OPT_COL_RADIX ? p->col_radix : p->row_radix) = value;
       return ES_OK;
+    case ES_OPT_OVERLAP:
+      if (value != 0 && value != 1) return fail(ES_E_ARG, "es_plan_set_option: overlap must be 0 or 1");
+      p->overlap = value;
+      return ES_OK;
+    case ES_OPT_ROW_CTAS:
+    case ES_OPT_COL_CTAS:
+      if (value < 0 || value > 16) return fail(ES_E_ARG, "es_plan_set_option: CTAs per SM must be in [0, 16]");
+      (option == ES_OPT_ROW_CTAS ? p->row_per_sm : p->col_per_sm) = value;
+      return ES_OK;
     default:
       return fail(ES_E_ARG, "es_plan_set_option: unknown option %d", option);
   }
@@ -883,6 +964,9 @@ int es_plan_get_option(es_plan* p, int option, int* value) {
     case ES_OPT_L2_HINTS: *value = p->l2_hints; return ES_OK;
     case ES_OPT_COL_RADIX: *value = p->col_radix; return ES_OK;
     case ES_OPT_ROW_RADIX: *value = p->row_radix; return ES_OK;
+    case ES_OPT_OVERLAP: *value = p->overlap; return ES_OK;
+    case ES_OPT_ROW_CTAS: *value = p->row_per_sm; return ES_OK;
+    case ES_OPT_COL_CTAS: *value = p->col_per_sm; return ES_OK;
     default: return fail(ES_E_ARG, "es_plan_get_option: unknown option %d", option);
   }
 }

@@ -80,6 +80,15 @@ int es_supported_sizes(int* sizes, int cap);
  * autotuner with the tile shapes. */
 #define ES_OPT_COL_RADIX 5
 #define ES_OPT_ROW_RADIX 6
+/* ES_OPT_OVERLAP (default 0): with 1, es_ionize alternates two intermediate spectra and runs the
+ * column passes (z inverse + filter, y inverse) of radius r + 1 on a stream the plan owns while the
+ * row pass of radius r runs on the caller's stream, ordered by events (no device-side waits); the
+ * call stays stream-ordered for the caller and can be captured in a CUDA graph.
+ * ES_OPT_ROW_CTAS / ES_OPT_COL_CTAS (0..16, default 0 = as many as fit): in overlap mode, caps on
+ * the resident CTAs per SM of the row and column passes, leaving room for the other stream's. */
+#define ES_OPT_OVERLAP 7
+#define ES_OPT_ROW_CTAS 8
+#define ES_OPT_COL_CTAS 9
 int es_plan_set_option(es_plan* plan, int option, int value);
 int es_plan_get_option(es_plan* plan, int option, int* value);
 /* Synchronises the stream and reports ES_E_DEVICE if any kernel of the plan gave up a bounded

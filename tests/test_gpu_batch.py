@@ -97,3 +97,28 @@ def test_batch_stalled_dependency_aborts_and_reports(mods):
         ok.run()
         ok.check()
         assert torch.isfinite(ok.nf).all()
+
+
+@pytest.mark.parametrize("overlap", [0, 1])
+def test_plan_graph_batch_matches_per_box_plans(mods, overlap):
+    # per-box plans on concurrent streams, captured in one CUDA graph and replayed twice, give the
+    # per-box plan's outputs bit for bit (same kernels, same grids, same reduction order)
+    eng, batch = mods
+    _lib = module("_lib")
+    boxes = _boxes(SPECS)
+    with batch.PlanGraphBatch(boxes, lanes=2, use_graph=True, tune=False) as g:
+        for _p, _s, _idx in g.lanes:
+            _p.set_option(_lib.OPT_OVERLAP, overlap)
+        g.run()
+        outs, nf = g.run()
+        g.check()
+        outs = [o.clone() for o in outs]
+        nf = nf.clone()
+        assert g.info()["lanes"] == sum(min(2, sum(1 for _, s in boxes if (s.n, s.box_len) == k))
+                                        for k in {(s.n, s.box_len) for _, s in boxes})
+    for i, (d, st) in enumerate(boxes):
+        with eng.ExcursionSetPlan(st.n, st.box_len) as p:
+            p.set_option(_lib.OPT_OVERLAP, overlap)
+            xh, nfp = p.run(d, st)
+        assert torch.equal(outs[i], xh), i
+        assert nf[i].item() == nfp.item(), i

@@ -139,6 +139,7 @@ def test_sphere_painting_matches_oracle(eng, ref_compat):
 def test_tile_variants_agree(eng, n, L):
     # every tile-shape candidate of the autotuner (TMA and synchronous passes) runs the same
     # transforms; they differ only in where the compiler contracts the filter multiply into FMAs
+    # and, with capped row-pass grids, in the order of the grid-wide erfc sum
     at = module("autotune")
     z = 8.0
     d = torch.from_numpy(grf.density_box(n, L, seed=1, z=z)).cuda()
@@ -146,8 +147,10 @@ def test_tile_variants_agree(eng, n, L):
     c = cos.brightness_temperature_factor(z, cos.BASELINE_COSMO)
     edges = sch.pk_edges(n, L, 20)
     outs = {}
+    # plus the overlapped-radius schedules on the first tile configuration
+    configs = list(at.CANDIDATES) + [at.with_overlap(at.CANDIDATES[0], ov) for ov in at.OVERLAP[1:]]
     with _plan(eng, n, L) as p:
-        for cfg in at.CANDIDATES:
+        for cfg in configs:
             at.apply(p, cfg)
             xh, nf = p.run(d, st)
             dT, ave = p.delta_T(xh, d, c)
