@@ -41,17 +41,18 @@ def ionize_setup(n, box_len, Z, p, *, fil, update, LE, scale=None, ref_compat=Fa
 
 _plans: "collections.OrderedDict" = collections.OrderedDict()
 _plans_lock = threading.Lock()
-MAX_CACHED_PLANS = 4
+MAX_CACHED_PLANS = 8
 
 
-def plan_for(n: int, box_len: float, max_radii: int, device):
-    """A cached ExcursionSetPlan for (n, box_len, device) with room for max_radii radii."""
+def plan_for(n: int, box_len: float, max_radii: int, device, lane: int = 0):
+    """A cached ExcursionSetPlan for (n, box_len, device) with room for max_radii radii; ``lane``
+    selects one of several plans of the same size (boxes running side by side)."""
     from ..engine import ExcursionSetPlan
     import torch
     dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
     if dev.index is None:
         dev = torch.device("cuda", torch.cuda.current_device())
-    key = (int(n), float(box_len), str(dev))
+    key = (int(n), float(box_len), str(dev), int(lane))
     with _plans_lock:
         plan = _plans.get(key)
         if plan is not None and plan.max_radii >= max_radii:

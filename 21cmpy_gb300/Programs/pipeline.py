@@ -48,15 +48,17 @@ def simulate_box(deltax, param_dict, Z=None, fil=0, update=0, LE=False, *, param
 
 
 def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=None, num_bins=None,
-                   ref_compat=False, xH_outs=None, dT_outs=None, device=None):
-    """``simulate_box`` for many boxes of one size, with the copies overlapped with the compute.
+                   ref_compat=False, xH_outs=None, dT_outs=None, device=None, lanes=3):
+    """``simulate_box`` for many boxes of one size, with the copies overlapped with the compute and
+    ``lanes`` boxes computed side by side.
 
     boxes: host (N, N, N) float32 boxes (pinned torch CPU tensors for the copies to overlap; numpy
-    arrays are pinned here first); Zs: their redshifts.  Box i + 1 is copied in and box i - 1's
-    x_HI and delta_T are copied out on their own streams while box i runs; two device slots of
-    each are reused, guarded by CUDA events.  x_HI and delta_T go to xH_outs / dT_outs (host
-    tensors; allocated pinned when not given).  Returns a list of dicts as ``simulate_box`` does,
-    with the boxes as torch CPU tensors; results are identical to box-by-box ``simulate_box``.
+    arrays are pinned here first); Zs: their redshifts.  Box i runs on lane i mod lanes (a plan and
+    a stream of its own); while it runs, later boxes are copied in and earlier boxes' x_HI and
+    delta_T are copied out on their own streams.  Each lane reuses two device slots per box
+    quantity, guarded by CUDA events.  x_HI and delta_T go to xH_outs / dT_outs (host tensors;
+    allocated pinned when not given).  Returns a list of dicts as ``simulate_box`` does, with the
+    boxes as torch CPU tensors; results are identical to box-by-box ``simulate_box``.
     """
     import torch
     p = _common.params(params)
@@ -66,6 +68,8 @@ def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=N
         raise ValueError("one redshift per box")
     if not boxes:
         return []
+    if lanes < 1:
+        raise ValueError("lanes must be >= 1")
     n = int(boxes[0].shape[0])
     if any(tuple(b.shape) != (n, n, n) or b.dtype != torch.float32 or b.is_cuda for b in boxes):
         raise ValueError("boxes must be host float32 (N, N, N) tensors or arrays of one size")
@@ -76,17 +80,24 @@ def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=N
     setups = [_common.ionize_setup(n, box_len, float(z), p, fil=fil, update=update, LE=LE, ref_compat=ref_compat)
               for z in Zs]
     consts = [cosmology.brightness_temperature_factor(float(z), cosmo) for z in Zs]
-    plan = _common.plan_for(n, box_len, max(s.n_radii for s in setups), device)
-    dev = plan.device
     nbox = len(boxes)
+    K = min(int(lanes), nbox)
+    radii = max(s.n_radii for s in setups)
+    plans = [_common.plan_for(n, box_len, radii, device, lane=k) for k in range(K)]
+    dev = plans[0].device
     xH_outs = xH_outs or [torch.empty((n, n, n), dtype=torch.float32).pin_memory() for _ in range(nbox)]
     dT_outs = dT_outs or [torch.empty((n, n, n), dtype=torch.float32).pin_memory() for _ in range(nbox)]
     with torch.cuda.device(dev):
-        comp = torch.cuda.current_stream(dev)
+        main = torch.cuda.current_stream(dev)
+        comps = [torch.cuda.Stream(dev) for _ in range(K)]
         s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-        d_in = [torch.empty((n, n, n), dtype=torch.float32, device=dev) for _ in range(2)]
-        d_xh = [torch.empty_like(d_in[0]) for _ in range(2)]
-        d_dT = [torch.empty_like(d_in[0]) for _ in range(2)]
+        fork = torch.cuda.Event()
+        fork.record(main)
+        for st_ in comps + [s_in, s_out]:
+            st_.wait_event(fork)
+        d_in = [torch.empty((n, n, n), dtype=torch.float32, device=dev) for _ in range(2 * K)]
+        d_xh = [torch.empty_like(d_in[0]) for _ in range(2 * K)]
+        d_dT = [torch.empty_like(d_in[0]) for _ in range(2 * K)]
         nf = torch.empty(nbox, dtype=torch.float32, device=dev)
         ave = torch.empty(nbox, dtype=torch.float32, device=dev)
         pk = torch.empty((nbox, 3, len(schedule.pk_k2_thresholds(n, box_len, np.asarray(edges)))),
@@ -95,15 +106,17 @@ def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=N
         ev_comp = [torch.cuda.Event() for _ in range(nbox)]
         ev_out = [torch.cuda.Event() for _ in range(nbox)]
         for i in range(nbox):
-            slot = i & 1
+            lane = i % K
+            slot = 2 * lane + ((i // K) & 1)                  # box i - 2K used this slot last
+            comp, plan = comps[lane], plans[lane]
             with torch.cuda.stream(s_in):
-                if i >= 2:
-                    s_in.wait_event(ev_comp[i - 2])           # box i - 2 no longer reads this slot
+                if i >= 2 * K:
+                    s_in.wait_event(ev_comp[i - 2 * K])       # box i - 2K no longer reads this slot
                 d_in[slot].copy_(boxes[i], non_blocking=True)
                 ev_in[i].record(s_in)
             comp.wait_event(ev_in[i])
-            if i >= 2:
-                comp.wait_event(ev_out[i - 2])                # box i - 2's outputs have left the slot
+            if i >= 2 * K:
+                comp.wait_event(ev_out[i - 2 * K])            # box i - 2K's outputs have left the slot
             plan.run(d_in[slot], setups[i], out=d_xh[slot], nf=nf[i:i + 1], output="xH", stream=comp)
             plan.delta_T(d_xh[slot], d_in[slot], consts[i], out=d_dT[slot], ave=ave[i:i + 1], stream=comp)
             plan.power_spectrum(d_dT[slot], ave[i:i + 1], edges, dimensional=bool(p["DIMENSIONAL_T_POWER_SPEC"]),
@@ -114,7 +127,8 @@ def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=N
                 xH_outs[i].copy_(d_xh[slot], non_blocking=True)
                 dT_outs[i].copy_(d_dT[slot], non_blocking=True)
                 ev_out[i].record(s_out)
-        comp.wait_stream(s_out)
+        for st_ in comps + [s_out]:
+            main.wait_stream(st_)
         nf_h, ave_h, pk_h = nf.cpu().numpy(), ave.cpu().numpy(), pk.cpu().numpy().astype(np.float64)
     return [{"xH": xH_outs[i], "dT": dT_outs[i], "nf": float(nf_h[i]), "ave": float(ave_h[i]), "K": edges,
              "k_ave": pk_h[i, 1], "ps_ave": pk_h[i, 0], "count": pk_h[i, 2], "n_radii": setups[i].n_radii}

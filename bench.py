@@ -33,6 +33,7 @@ METRIC = "voxel-radius updates/s @256^3 (fused excursion-set engine)"
 UNIT = "voxel-radius updates/s"
 N = 256
 BOX_LEN = 300.0
+LANES = 3                 # boxes in flight per GPU, each on its own plan and stream
 NUM_BINS = 20
 
 # Algorithmic bytes per voxel for one launch of each kernel kind: what the kernel must read and
@@ -241,16 +242,30 @@ def main():
     nf = torch.empty((nboxes, 1), dtype=torch.float32, device=dev)
     ave = torch.empty((nboxes, 1), dtype=torch.float32, device=dev)
     pk = torch.empty((nboxes, 3, NUM_BINS), dtype=torch.float32, device=dev)
+    at = importlib.import_module("21cmpy_gb300.autotune")
     plan = eng.ExcursionSetPlan(N, BOX_LEN, max_radii=64, device=dev)
-    tuned = importlib.import_module("21cmpy_gb300.autotune").ensure_tuned(plan)
+    tuned = at.ensure_tuned(plan)
+    # boxes are independent: LANES plans, each on its own stream, take boxes in turn
+    plans = [plan] + [eng.ExcursionSetPlan(N, BOX_LEN, max_radii=64, device=dev) for _ in range(LANES - 1)]
+    for p_ in plans[1:]:
+        at.apply(p_, tuned["config"])
+    lane_streams = [torch.cuda.Stream(dev) for _ in plans]
     updates_per_step = sum(N ** 3 * st.n_radii for st, _c in setups)
 
     def step():
+        main = torch.cuda.current_stream(dev)
+        fork = torch.cuda.Event()
+        fork.record(main)
+        for s_ in lane_streams:
+            s_.wait_event(fork)
         for i in range(nboxes):
             st, c = setups[i]
-            plan.run(dens[i], st, out=xh[i], nf=nf[i])
-            plan.delta_T(xh[i], dens[i], c, out=dT[i], ave=ave[i])
-            plan.power_spectrum(dT[i], ave[i], edges, out=pk[i])
+            p_, s_ = plans[i % LANES], lane_streams[i % LANES]
+            p_.run(dens[i], st, out=xh[i], nf=nf[i], stream=s_)
+            p_.delta_T(xh[i], dens[i], c, out=dT[i], ave=ave[i], stream=s_)
+            p_.power_spectrum(dT[i], ave[i], edges, out=pk[i], stream=s_)
+        for s_ in lane_streams:
+            main.wait_stream(s_)
 
     def barrier():
         if dist is not None:
@@ -276,7 +291,8 @@ def main():
     # the same K steps again with a CUDA event pair around every launch on the plan's stream: the
     # per-kernel times (kernel_ms, roofline) of this instrumented pass
     launches_per_box = 3 + 1 + 3 * max(st.n_radii for st, _c in setups) + 1 + 1 + 3
-    plan.profile_enable(launches_per_box * nboxes * args.steps + 16)
+    for p_ in plans:
+        p_.profile_enable(launches_per_box * nboxes * args.steps + 16)
     barrier()
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)
@@ -287,8 +303,12 @@ def main():
     barrier()
     elapsed_profiled = e2.elapsed_time(e3) / 1e3
     clock_info = clocks.stop()
-    prof = plan.profile_read()
-    plan.profile_enable(0)
+    prof = {}
+    for p_ in plans:
+        for k, (ms_, cnt_) in p_.profile_read().items():
+            a_ms, a_cnt = prof.get(k, (0.0, 0))
+            prof[k] = (a_ms + ms_, a_cnt + cnt_)
+        p_.profile_enable(0)
     if dist is not None:
         t = torch.tensor([elapsed], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -307,26 +327,30 @@ def main():
     path_bytes = (B_RADIUS * N ** 3 * radii_total + (B_BOX + B_DT_PK) * N ** 3 * nboxes) * args.steps * world
     path_gbs = path_bytes / elapsed / 1e9
 
-    # with overlapped radii the row pass shares the GPU with the next radius' column passes, so its
-    # live launch time includes co-running work; one more instrumented step with the overlap off
-    # gives the same kernel's time alone
-    roofline_isolated = None
+    # boxes run side by side and, with overlapped radii, the row pass shares the GPU with the next
+    # radius' column passes, so live launch times include co-running work; one more instrumented
+    # step, boxes in turn on one plan with the overlap off, gives the same kernel's time alone
     lib_consts = importlib.import_module("21cmpy_gb300._lib")
-    overlapped = plan.get_option(lib_consts.OPT_OVERLAP) == 1
+    overlapped = plan.get_option(lib_consts.OPT_OVERLAP) == 1 or LANES > 1
+    roofline_isolated = None
     if overlapped:
+        ov_old = plan.get_option(lib_consts.OPT_OVERLAP)
         plan.set_option(lib_consts.OPT_OVERLAP, 0)
         plan.profile_enable(launches_per_box * nboxes + 16)
         barrier()
-        step()
+        for i in range(nboxes):
+            st, c = setups[i]
+            plan.run(dens[i], st, out=xh[i], nf=nf[i])
+            plan.delta_T(xh[i], dens[i], c, out=dT[i], ave=ave[i])
+            plan.power_spectrum(dT[i], ave[i], edges, out=pk[i])
         barrier()
         prof_iso = plan.profile_read()
         plan.profile_enable(0)
-        plan.set_option(lib_consts.OPT_OVERLAP, 1)
+        plan.set_option(lib_consts.OPT_OVERLAP, ov_old)
         iso_ms, iso_count = prof_iso[dom]
         iso_gbs = dom_bytes * iso_count / (iso_ms / 1e3) / 1e9
         roofline_isolated = {"kernel": dom, "achieved": iso_gbs, "peak": hbm, "unit": "GB/s", "frac": iso_gbs / hbm,
-                             "launch_ms": iso_ms / iso_count,
-                             "note": "one step with overlapped radii off: the kernel alone on the GPU"}
+                             "launch_ms": iso_ms / iso_count}
 
     # end-to-end through the public host-buffer API (pinned host inputs/outputs)
     e2e = None
@@ -356,21 +380,19 @@ def main():
                    "n": N, "box_len_mpc": BOX_LEN, "boxes_per_gpu": nboxes, "radii_per_box": radii_total // nboxes,
                    "l2": "no flush: every box's inputs (64 MiB density + 64 MiB spectrum) and its 256 MiB working "
                          "set exceed the 129 MB L2, and consecutive boxes touch different inputs",
-                   "parallelism": f"{world} independent GPU(s), boxes sharded by seed, no collective"},
+                   "parallelism": f"{world} independent GPU(s), boxes sharded by seed, no collective; "
+                                  f"{LANES} boxes side by side per GPU (one plan and stream each)"},
         "gpu_launches": int(sum(c for _ms, c in prof.values())),
         "autotune": {"config": tuned.get("config"), "source": tuned.get("source"),
                      "meaning": "(pass variant, column tile, row tile, column radix schedule, row radix schedule, overlapped radii, row-pass CTAs per SM, column-pass CTAs per SM)"},
         "kernel_ms": {k: round(v[0], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "kernel_ms_note": f"per-launch CUDA events over a second pass of the same {args.steps} steps "
                           f"({1e3 * elapsed_profiled / args.steps:.1f} ms per step with the events)"
-                          + ("; radii overlap on two streams (column passes of radius r + 1 beside the row "
-                             "pass of radius r), so a launch's time includes the work running beside it"
-                             if overlapped else ""),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": f"{peak_kind} hbm_gbs",
-                     "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": dom_ms / dom_count,
-                     "traffic": traffic},
-        "roofline_isolated": roofline_isolated,
+                          + (f"; {LANES} boxes run side by side on their own plans and streams, and radii overlap "
+                             "(column passes of radius r + 1 beside the row pass of radius r), so a launch's time "
+                             "includes the work running beside it" if overlapped else ""),
+        "roofline": roofline_line(dom, dom_bytes, dom_ms, dom_count, achieved, hbm, peak_kind, traffic,
+                                  roofline_isolated, prof, elapsed_profiled, args.steps),
         "path_roofline": {"achieved": path_gbs, "peak": hbm, "unit": "GB/s", "frac": path_gbs / hbm,
                           "bytes_model": "22 B/voxel-radius + 20 B/voxel-box + 24 B/voxel delta_T+P(k)"},
         "clocks": clock_info,
@@ -387,11 +409,41 @@ def main():
         line["cpu_baseline"] = cpu_baseline(work, setups, args.cpu_radii)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    plan.close()
+    for p_ in plans:
+        p_.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
 
+
+
+def roofline_line(dom, dom_bytes, dom_ms, dom_count, achieved, hbm, peak_kind, traffic, iso, prof,
+                  elapsed_profiled, steps):
+    """The dominant kernel's roofline.  With boxes side by side and overlapped radii, an event pair
+    around a launch also spans the work of the other streams, so the kernel's own rate comes from
+    one extra step run serially (one plan, boxes in turn, radii not overlapped); the live
+    event-bracketed rate and the wall time apportioned by the kernel's share of event time are
+    given beside it."""
+    live = {"achieved": achieved, "frac": achieved / hbm, "launch_ms": dom_ms / dom_count,
+            "measured": "CUDA event pair around each launch in the instrumented pass of the concurrent "
+                        "schedule (spans the work running beside it on other streams)"}
+    share = dom_ms / sum(ms for ms, _c in prof.values())
+    app_ms = 1e3 * elapsed_profiled * share / dom_count
+    apportioned = {"achieved": dom_bytes / (app_ms / 1e3) / 1e9, "frac": dom_bytes / (app_ms / 1e3) / 1e9 / hbm,
+                   "launch_ms": app_ms, "share_of_event_time": share,
+                   "measured": "wall time of the instrumented pass times the kernel's share of all launches' "
+                               "event time, per launch"}
+    line = {"bound": "hbm", "kernel": dom, "peak": hbm, "unit": "GB/s", "peak_source": f"{peak_kind} hbm_gbs",
+            "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic}
+    if iso is None:
+        line.update({"achieved": achieved, "frac": achieved / hbm, "launch_ms": dom_ms / dom_count,
+                     "measured": "CUDA event pair around each launch, instrumented pass of the same steps"})
+        return line
+    line.update({"achieved": iso["achieved"], "frac": iso["frac"], "launch_ms": iso["launch_ms"],
+                 "measured": "CUDA event pair around each launch of one extra step of the same boxes run "
+                             "serially on one plan (boxes in turn, radii not overlapped): the kernel alone",
+                 "live": live, "apportioned": apportioned})
+    return line
 
 def run_e2e(args, work, dev, barrier, dist):
     import torch
@@ -428,7 +480,7 @@ def run_e2e(args, work, dev, barrier, dist):
     return {"value": N ** 3 * radii * world / dt, "unit": UNIT, "h2d_bytes_per_step": nb * N ** 3 * 4,
             "d2h_bytes_per_step": nb * (2 * N ** 3 * 4 + 3 * NUM_BINS * 4 + 8),
             "api": "Programs.pipeline.simulate_sweep (find_HII_bubbles + delta_T of every box on pinned host "
-                   "buffers, copies overlapped with compute)",
+                   "buffers, copies overlapped with compute, 3 boxes side by side)",
             "ms_per_step": 1e3 * dt / args.steps}
 
 
