@@ -209,6 +209,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven batched-sweep measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-speed measurement")
     ap.add_argument("--no-perturb", action="store_true", help="skip the density-evolution measurement")
+    ap.add_argument("--no-config3", action="store_true", help="skip the single 512^3 box measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
@@ -364,6 +365,9 @@ def main():
     surrogate_info = None
     if not args.no_surrogate and world == 1:
         surrogate_info = run_surrogate(dev)
+    config3_info = None
+    if not args.no_config3 and world == 1:
+        config3_info = run_config3(dev, hbm)
     perturb_info = None
     if not args.no_perturb and world == 1:
         perturb_info = run_perturb(dev, hbm)
@@ -403,6 +407,8 @@ def main():
         line["batched_sweep"] = batch_info
     if surrogate_info is not None:
         line["surrogate"] = surrogate_info
+    if config3_info is not None:
+        line["box_512"] = config3_info
     if perturb_info is not None:
         line["perturb_field"] = perturb_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -483,6 +489,94 @@ def run_e2e(args, work, dev, barrier, dist):
                    "buffers, copies overlapped with compute, 3 boxes side by side)",
             "ms_per_step": 1e3 * dt / args.steps}
 
+
+
+def run_config3(dev, hbm_gbs: float, reps: int = 3):
+    """One 512^3 box (BOX_LEN = 600 Mpc, z = 7.5, zeta = 40, R_mfp = 30 Mpc, 40 radii): time per box,
+    per-pass HBM GB/s from one serial instrumented box, and the engine's plain 3-D real FFTs next to
+    torch.fft (cuFFT), which is timed here as a yardstick only."""
+    import numpy as np
+    import torch
+    eng = importlib.import_module("21cmpy_gb300.engine")
+    at = importlib.import_module("21cmpy_gb300.autotune")
+    grf = importlib.import_module("21cmpy_gb300.grf")
+    sch = importlib.import_module("21cmpy_gb300.schedule")
+    cos = importlib.import_module("21cmpy_gb300.cosmology")
+    lib_consts = importlib.import_module("21cmpy_gb300._lib")
+    n, L, z = 512, 600.0, 7.5
+    d = torch.from_numpy(grf.density_box(n, L, 0, z)).to(dev)
+    st = sch.ionize_setup(n, L, z, zeta=40.0, t_vir_min=1e4, R_max=30.0, cosmo=cos.BASELINE_COSMO)
+    c = cos.brightness_temperature_factor(z, cos.BASELINE_COSMO)
+    edges = sch.pk_edges(n, L, NUM_BINS)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    with eng.ExcursionSetPlan(n, L, max_radii=64, device=dev) as plan:
+        tuned = at.ensure_tuned(plan)
+        xh, dT = torch.empty_like(d), torch.empty_like(d)
+
+        def box():
+            plan.run(d, st, out=xh)
+            _, ave = plan.delta_T(xh, d, c, out=dT)
+            plan.power_spectrum(dT, ave, edges)
+
+        box()
+        torch.cuda.synchronize(dev)
+        e0, e1 = ev(), ev()
+        e0.record()
+        for _ in range(reps):
+            box()
+        e1.record()
+        e1.synchronize()
+        ms_box = e0.elapsed_time(e1) / reps
+        # per pass, one box run serially (radii not overlapped) with an event pair per launch
+        ov = plan.get_option(lib_consts.OPT_OVERLAP)
+        plan.set_option(lib_consts.OPT_OVERLAP, 0)
+        plan.profile_enable(4 * 64 + 32)
+        box()
+        torch.cuda.synchronize(dev)
+        prof = plan.profile_read()
+        plan.profile_enable(0)
+        plan.set_option(lib_consts.OPT_OVERLAP, ov)
+        half = 8.0 * (n // 2 + 1) / n
+        bpv = {"col_z_inv_filter": 2 * half, "col_y_inv": 2 * half, "row_c2r_ionize": half + 8.25}
+        passes = {}
+        for k, b in bpv.items():
+            ms, cnt = prof[k]
+            us = 1e3 * ms / cnt
+            gbs = b * n ** 3 / (us / 1e6) / 1e9
+            passes[k] = {"us_per_launch": round(us, 2), "GB_s": round(gbs, 1), "frac": round(gbs / hbm_gbs, 3),
+                         "algorithmic_bytes_per_voxel": round(b, 3)}
+
+        # plain 3-D real FFTs: the engine's three passes against cuFFT through torch.fft
+        def timed(fn, k=5):
+            fn()
+            torch.cuda.synchronize(dev)
+            a, b = ev(), ev()
+            a.record()
+            for _ in range(k):
+                fn()
+            b.record()
+            b.synchronize()
+            return a.elapsed_time(b) / k
+
+        X = plan.fft_r2c(d)
+        ms_r2c = timed(lambda: plan.fft_r2c(d))
+        ms_c2r = timed(lambda: plan.fft_c2r(X))
+        ms_r2c_cufft = timed(lambda: torch.fft.rfftn(d))
+        Xt = torch.fft.rfftn(d)
+        ms_c2r_cufft = timed(lambda: torch.fft.irfftn(Xt, s=(n, n, n)))
+        del X, Xt
+    fft_bytes = (4.0 + half) * n ** 3              # read one array, write the other
+    gb = lambda ms: round(fft_bytes / (ms / 1e3) / 1e9, 1)
+    return {"workload": "one 512^3 box, BOX_LEN=600 Mpc, z=7.5, zeta=40, R_mfp=30 Mpc, Tvir=1e4 K, "
+                        f"{st.n_radii} radii, delta_T + {NUM_BINS}-bin P(k)",
+            "ms_per_box": ms_box, "value": n ** 3 * st.n_radii / (ms_box / 1e3), "unit": UNIT,
+            "autotune": tuned.get("config"), "passes": passes,
+            "passes_note": "one box run serially (radii not overlapped), CUDA event pair per launch",
+            "fft_yardstick": {"engine_r2c_ms": ms_r2c, "engine_c2r_ms": ms_c2r, "cufft_r2c_ms": ms_r2c_cufft,
+                              "cufft_c2r_ms": ms_c2r_cufft, "engine_r2c_GB_s": gb(ms_r2c), "engine_c2r_GB_s": gb(ms_c2r),
+                              "cufft_r2c_GB_s": gb(ms_r2c_cufft), "cufft_c2r_GB_s": gb(ms_c2r_cufft),
+                              "bytes_model": "4 B real + 8 (n/2+1)/n B half spectrum per voxel",
+                              "note": "cuFFT (torch.fft) is timed as a yardstick only; it is not on any path"}}
 
 def run_perturb(dev, hbm_gbs: float, reps: int = 20):
     """Zel'dovich move of a 512^3 initial-conditions box onto a 128^3 grid (the reference's default
