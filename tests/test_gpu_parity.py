@@ -282,3 +282,29 @@ def test_full_size_256_box_matches_oracle(eng):
     with _plan(eng, b.n, b.box_len) as p:
         out, _ = p.run(torch.from_numpy(d).cuda(), st, output="ionized")
     _compare_ionized(out.cpu().numpy().astype(np.float64), ref, "256^3")
+
+
+@pytest.mark.parametrize("update", [0, 1])
+def test_overlapped_radii_match_serial_schedule(eng, update):
+    # the column passes of radius r + 1 on the plan's own stream beside the row pass (and, in
+    # sphere mode, the painting) of radius r: the same flags and x_HI as the serial schedule, and
+    # the oracle's, for centre and sphere updates; capped grids only reorder the erfc sum
+    _lib = module("_lib")
+    n, L, z = 96, 144.0, 8.0
+    d = grf.density_box(n, L, seed=21, z=z)
+    st = _setup(n, L, z, update=update, R_max=12.0)
+    dd = torch.from_numpy(d).cuda()
+    with _plan(eng, n, L) as p:
+        serial, _ = p.run(dd, st, output="ionized")
+        serial = serial.clone()
+        for ov in ((1, 0, 0), (1, 1, 2), (1, 2, 1)):
+            for opt, v in zip((_lib.OPT_OVERLAP, _lib.OPT_ROW_CTAS, _lib.OPT_COL_CTAS), ov):
+                p.set_option(opt, v)
+            out, _ = p.run(dd, st, output="ionized")
+            if ov[1] == 0:
+                assert torch.equal(out, serial), ov
+            else:
+                assert (out != serial).float().mean().item() <= 1e-4, ov
+        p.check()
+    ref = O.conv_bubbles(d, st, tol=FLAG_TOL)
+    _compare_ionized(out.cpu().numpy().astype(np.float64), ref, f"overlap update={update}")
