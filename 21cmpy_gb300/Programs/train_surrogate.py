@@ -59,7 +59,8 @@ def main(argv=None):
     losses = []
     for ep in range(args.epochs):
         perm = order_rng.permutation(len(train))
-        losses.extend(S.train(net, [train[i] for i in perm], epochs=1, lr=args.lr * (0.7 ** ep), log=log))
+        losses.extend(S.train(net, [train[i] for i in perm], epochs=1, lr=args.lr * (0.7 ** ep),
+                              log=lambda m, ep=ep: log(m.replace("epoch 0:", f"epoch {ep}:", 1))))
     torch.cuda.synchronize()
     t_train = time.time() - t0
     trained = S.evaluate(net, held, gen.plan)
