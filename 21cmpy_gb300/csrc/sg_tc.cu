@@ -36,6 +36,7 @@
 
 #include <cstdio>
 #include <string>
+#include <type_traits>
 
 #include "es_engine.h"
 
@@ -333,21 +334,28 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __nv_bfloat16
           const uint32_t d1 = tmem + (uint32_t)(s0 * COUT);
           const uint64_t a_g = a_base + (uint64_t)((g % YS) * (3 * L::ROW_BYTES / 16));
           const uint64_t b_blk = b_base + (uint64_t)((Y - yhi + 1) * COUT);   // first dy block, 16-byte units
+// One straight run of MMAs per case: a test between the MMAs (whether the slot ring wraps)
+          // would put a branch around every elected issue and slow the issue to ~90 cycles per MMA;
+          // without it the issue keeps pace with the tensor pipe (~56 cycles at N = 96).
+          auto issue = [&](auto two) {
+            constexpr bool TWO = decltype(two)::value;
 #pragma unroll
-          for (int dz = 0; dz < 3; ++dz) {
+            for (int dz = 0; dz < 3; ++dz) {
 #pragma unroll
-            for (int dx = 0; dx < 3; ++dx) {
-              const uint64_t ad = a_g + (uint64_t)((dz * L::ROW_BYTES + (XOFF + dx - 1) * 16) / 16);
-              const uint64_t bd = b_blk + (uint64_t)((dz * 3 + dx) * L::PAIR_B / 16);
+              for (int dx = 0; dx < 3; ++dx) {
+                const uint64_t ad = a_g + (uint64_t)((dz * L::ROW_BYTES + (XOFF + dx - 1) * 16) / 16);
+                const uint64_t bd = b_blk + (uint64_t)((dz * 3 + dx) * L::PAIR_B / 16);
 #pragma unroll
-              for (int k = 0; k < KSTEPS; ++k) {
-                const uint64_t ak = ad + (uint64_t)(2 * k * CHUNK / 16);
-                const uint64_t bk = bd + (uint64_t)(2 * k * L::LBO_B / 16);
-                mma_acc(d1, ak, bk, id1);
-                if (n2 > 0) mma_acc(tmem, ak, bk + (uint64_t)(n1 * COUT), id2);
+                for (int k = 0; k < KSTEPS; ++k) {
+                  const uint64_t ak = ad + (uint64_t)(2 * k * CHUNK / 16);
+                  const uint64_t bk = bd + (uint64_t)(2 * k * L::LBO_B / 16);
+                  mma_acc(d1, ak, bk, id1);
+                  if (TWO) mma_acc(tmem, ak, bk + (uint64_t)(n1 * COUT), id2);
+                }
               }
             }
-          }
+          };
+          if (n2 > 0) issue(std::true_type{}); else issue(std::false_type{});
           mma_commit(&sfree[g % YS]);                 // this input group is not read again
           if (Y - 1 >= yb && Y - 1 < ye) {
             const int od = o0 + (Y - 1 - yb);          // output row Y - 1 has all 27 taps
