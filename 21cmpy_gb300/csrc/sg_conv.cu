@@ -293,6 +293,21 @@ int launch_wgrad(int n, const void* x, const void* dz, float* dw, float* db, flo
 }
 
 bool shape_ok(int n) { return n >= 16 && n <= sg::MAXN && n % 16 == 0; }
+
+// Network input: 16 BF16 channels per voxel, channel 0 = bf16(delta * scale), channels 1..15 the
+// constant bit patterns in c (channel 0 of c is ignored); two 16-byte stores per voxel.
+struct Feat16 {
+  uint32_t w[8];
+};
+__global__ void features_kernel(long voxels, const float* __restrict__ delta, float scale, Feat16 c,
+                                uint4* __restrict__ out) {
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < voxels; v += (long)gridDim.x * blockDim.x) {
+    const __nv_bfloat16 d0 = __float2bfloat16_rn(__ldg(delta + v) * scale);
+    const uint32_t lo = (uint32_t)__bfloat16_as_ushort(d0) | (c.w[0] & 0xFFFF0000u);
+    out[2 * v] = make_uint4(lo, c.w[1], c.w[2], c.w[3]);
+    out[2 * v + 1] = make_uint4(c.w[4], c.w[5], c.w[6], c.w[7]);
+  }
+}
 std::atomic<int> g_impl{SG_IMPL_AUTO};
 }  // namespace
 
@@ -342,6 +357,22 @@ size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout) {
   int chunks = (sms * 2 + 8) / 9;
   if (chunks > n * n) chunks = n * n;
   return (size_t)9 * chunks * (27 * cout * cin + cout) * sizeof(float);
+}
+
+int sg_features(int n, const float* delta, float scale, const uint16_t* channels16, void* out, void* stream) {
+  if (n < 1 || n > 2048 || !delta || !channels16 || !out) return sgfail(ES_E_ARG, "sg_features: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(out) & 15u) != 0) return sgfail(ES_E_ARG, "sg_features: out must be 16-byte aligned");
+  Feat16 c;
+  for (int i = 0; i < 8; ++i) c.w[i] = (uint32_t)channels16[2 * i] | ((uint32_t)channels16[2 * i + 1] << 16);
+  const long voxels = (long)n * n * n;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long blocks = (voxels + 255) / 256;
+  if (blocks > (long)sms * 16) blocks = (long)sms * 16;
+  features_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(voxels, delta, scale, c, (uint4*)out);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ES_OK : sgfail(ES_E_CUDA, "sg_features launch: %s", cudaGetErrorString(e));
 }
 
 int sg_conv3d_set_impl(int impl) {

@@ -52,6 +52,7 @@ class SurrogateNet:
             self.w.append(w.to(self.device).requires_grad_(False))
             self.b.append(torch.zeros(cout, device=self.device))
         self._ws = None
+        self._wb, self._wb_key = None, None
 
     def parameters(self):
         return self.w + self.b
@@ -80,12 +81,21 @@ class SurrogateNet:
         rc = self.lib.sg_conv3d_wgrad(n, cin, cout, _p(x), _p(dz), _p(dw), _p(db), _p(self._ws), need, _stream())
         _lib.check("sg_conv3d_wgrad", rc, self.lib)
 
+    def bf16_weights(self):
+        """BF16 copies of the FP32 master weights, converted again only after a weight changed (in
+        place, as the optimiser and load_state change them: tracked by the tensors' versions)."""
+        key = tuple((w.data_ptr(), w._version) for w in self.w)
+        if self._wb_key != key:
+            self._wb = [w.to(torch.bfloat16).contiguous() for w in self.w]
+            self._wb_key = key
+        return self._wb
+
     def forward(self, feats: torch.Tensor, keep: bool = False):
         """feats: bf16 [n, n, n, 16].  Returns (x_HI float [n, n, n], activations if keep)."""
         n = feats.shape[0]
         acts = [feats]
         x = feats
-        wb = [w.to(torch.bfloat16).contiguous() for w in self.w]
+        wb = self.bf16_weights()
         for li, (cin, cout) in enumerate(LAYERS[:-1]):
             y = torch.empty((n, n, n, cout), dtype=torch.bfloat16, device=self.device)
             self._conv(n, cin, cout, 0, x, wb[li], self.b[li], y)
@@ -125,11 +135,18 @@ def features(delta: torch.Tensor, z: float, zeta: float, R_max: float, t_vir: fl
              cosmo=cosmology.BASELINE_COSMO) -> torch.Tensor:
     """bf16 [n, n, n, 16] network input for a density box at redshift z and a parameter point."""
     n = delta.shape[0]
+    if not (isinstance(delta, torch.Tensor) and delta.is_cuda and delta.dtype == torch.float32
+            and delta.is_contiguous() and tuple(delta.shape) == (n, n, n)):
+        raise ValueError("delta must be a contiguous float32 (n, n, n) CUDA tensor")
     const = torch.zeros(16, dtype=torch.float32)
     const[1:5] = torch.tensor([zeta / 80.0, R_max / 50.0, math.log10(t_vir) - 4.0, (z - 6.0) / 4.0])
+    bits = (C.c_uint16 * 16)(*[int(v) & 0xFFFF for v in const.to(torch.bfloat16).view(torch.int16).tolist()])
+    scale = float(np.float32(1.0 / (4.0 * cosmology.growth_factor(z, cosmo))))
     f = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=delta.device)
-    f[...] = const.to(device=delta.device, dtype=torch.bfloat16)
-    f[..., 0] = (delta / cosmology.growth_factor(z, cosmo) / 4.0).to(torch.bfloat16)
+    lib = _lib.load()
+    with torch.cuda.device(delta.device):
+        rc = lib.sg_features(n, _p(delta), C.c_float(scale), bits, _p(f), _stream())
+    _lib.check("sg_features", rc, lib)
     return f
 
 

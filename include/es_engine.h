@@ -209,6 +209,10 @@ int sg_conv3d_fwd(int n, int cin, int cout, int mode, const void* in, const void
 int sg_conv3d_wgrad(int n, int cin, int cout, const void* x, const void* dz, float* dw, float* db,
                     float* ws, size_t ws_bytes, void* stream);
 size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout);
+/* Network input for one box: out[n^3][16] bf16 with channel 0 = bf16(delta * scale) (round to
+ * nearest even) and channels 1..15 = channels16[1..15] (bf16 bit patterns; channels16[0] unused).
+ * delta: float [n^3] on the device; out 16-byte aligned. */
+int sg_features(int n, const float* delta, float scale, const uint16_t* channels16, void* out, void* stream);
 /* Which kernels sg_conv3d_fwd runs (process-wide, no counterpart in the reference):
  * SG_IMPL_AUTO = tcgen05/TMEM kernels for n = 128 (one CTA per SM, TMA-fed, accumulators in tensor
  * memory) and mma.sync kernels for other n; SG_IMPL_MMA_SYNC = mma.sync kernels for every n. */

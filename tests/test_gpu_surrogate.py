@@ -214,3 +214,25 @@ def test_sweep_uses_the_engine_as_fallback_and_judge(sg):
     sweep = sg.SurrogateSweep(net, gen, max_abs_err=1.0, check_every=0)
     far = dict(pts[0], zeta=200.0)
     assert sweep(deltas[0], far)[1] == "engine" and sweep.fallbacks == 1
+
+
+def test_features_kernel_and_cached_weights(sg):
+    # the fused input kernel: channel 0 = bf16(delta * scale) rounded to nearest even, channels
+    # 1..4 the parameter constants, the rest zero; the BF16 weight copies follow in-place updates
+    cosm = module("cosmology")
+    n = 32
+    delta = torch.randn((n,) * 3, device="cuda") * 2.0
+    z, zeta, rmax, tvir = 8.0, 30.0, 15.0, 2e4
+    f = sg.features(delta, z, zeta, rmax, tvir)
+    scale = np.float32(1.0 / (4.0 * cosm.growth_factor(z, cosm.BASELINE_COSMO)))
+    ref0 = (delta * torch.tensor(float(scale), device="cuda")).to(torch.bfloat16)
+    assert torch.equal(f[..., 0], ref0)
+    const = torch.tensor([zeta / 80.0, rmax / 50.0, np.log10(tvir) - 4.0, (z - 6.0) / 4.0]).to(torch.bfloat16)
+    assert torch.equal(f[..., 1:5], const.cuda().expand(n, n, n, 4))
+    assert not f[..., 5:].any()
+    net = sg.SurrogateNet(seed=0)
+    w0 = net.bf16_weights()
+    assert net.bf16_weights() is w0
+    net.w[3].mul_(0.5)
+    w1 = net.bf16_weights()
+    assert w1 is not w0 and torch.equal(w1[3], net.w[3].to(torch.bfloat16))
