@@ -3,6 +3,7 @@
 // [element][row] layout (pitch RL + 1, so every Stockham stage reads and writes shared memory
 // without bank conflicts) and leave through coalesced stores.
 #pragma once
+#include <type_traits>
 #include "es_tma.cuh"
 
 namespace es {
@@ -136,35 +137,44 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
       }
     } else {
       const float2* pv = s ? P1 : P0;
-      for (int e = threadIdx.x; e < RL * M; e += T) {     // whole warps: 64 consecutive voxels
-        const int row = e / M, p = e % M;
-        const float2 d = Zr[p * ES + row];
-        acc += erfc_sum_term((dc - d.x) * inv_denom) + erfc_sum_term((dc - d.y) * inv_denom);
-        if (has_prev) {
-          const float2 pp = pv[e];
-          const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
-          const unsigned bx = __ballot_sync(0xffffffffu, px);
-          const unsigned by = __ballot_sync(0xffffffffu, py);
-          if (a.update == 0) {
-            // pair-major bitmap: one 64-bit word per 32 pairs, even voxels in the low half;
-            // a fire-and-forget OR, so nothing on the warp's path waits for memory
-            if (lane == 0 && (bx | by))
-              atomicOr(reinterpret_cast<unsigned long long*>(a.flags) + (pair0 + e) / 32,
-                       ((unsigned long long)by << 32) | bx);
-          } else if (bx | by) {
-            const unsigned cnt = __popc(bx) + __popc(by);
-            unsigned first = 0;
-            if (lane == 0) first = atomicAdd(a.center_count, cnt);
-            first = __shfl_sync(0xffffffffu, first, 0);
-            const unsigned lt = (1u << lane) - 1u;
-            const unsigned v0 = (unsigned)((pair0 + e) * 2);
-            unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
-            if (px) a.centers[pos++] = v0;
-            if (py) a.centers[pos] = v0 + 1;
+      // one loop per (previous radius present, update mode): tests that are uniform over the
+      // launch stay out of the loop body
+      auto epilogue = [&](auto hp, auto upd) {
+        constexpr bool HP = decltype(hp)::value;
+        constexpr int UPD = decltype(upd)::value;
+        for (int e = threadIdx.x; e < RL * M; e += T) {     // whole warps: 64 consecutive voxels
+          const int row = e / M, p = e % M;
+          const float2 d = Zr[p * ES + row];
+          acc += erfc_sum_term((dc - d.x) * inv_denom) + erfc_sum_term((dc - d.y) * inv_denom);
+          if (HP) {
+            const float2 pp = pv[e];
+            const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
+            const unsigned bx = __ballot_sync(0xffffffffu, px);
+            const unsigned by = __ballot_sync(0xffffffffu, py);
+            if (UPD == 0) {
+              // pair-major bitmap: one 64-bit word per 32 pairs, even voxels in the low half;
+              // a fire-and-forget OR, so nothing on the warp's path waits for memory
+              if (lane == 0 && (bx | by))
+                atomicOr(reinterpret_cast<unsigned long long*>(a.flags) + (pair0 + e) / 32,
+                         ((unsigned long long)by << 32) | bx);
+            } else if (bx | by) {
+              const unsigned cnt = __popc(bx) + __popc(by);
+              unsigned first = 0;
+              if (lane == 0) first = atomicAdd(a.center_count, cnt);
+              first = __shfl_sync(0xffffffffu, first, 0);
+              const unsigned lt = (1u << lane) - 1u;
+              const unsigned v0 = (unsigned)((pair0 + e) * 2);
+              unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
+              if (px) a.centers[pos++] = v0;
+              if (py) a.centers[pos] = v0 + 1;
+            }
           }
+          __stcs(a.rout + pair0 + e, d);                 // streamed: read again only next radius
         }
-        __stcs(a.rout + pair0 + e, d);                 // streamed: read again only next radius
-      }
+      };
+      if (!has_prev) epilogue(std::false_type{}, std::integral_constant<int, 0>{});
+      else if (a.update == 0) epilogue(std::true_type{}, std::integral_constant<int, 0>{});
+      else epilogue(std::true_type{}, std::integral_constant<int, 1>{});
     }
     __syncthreads();                                   // S[s], P[s], A, B free again
     if (threadIdx.x == 0 && it + 2 < my_count) {
