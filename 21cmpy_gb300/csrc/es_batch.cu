@@ -120,18 +120,23 @@ __device__ __noinline__ void b_col(const BoxDev& b, int radius, int tile, float2
   const float2* src = OP == B_COL_Z_INV ? (nyq ? b.Xnyq : b.X) : (nyq ? b.Tnyq : b.T);
   if (OP == B_COL_Y_FWD || OP == B_COL_Z_FWD) src = nyq ? b.Xnyq : b.X;
   float2* dst = OP == B_COL_Y_FWD || OP == B_COL_Z_FWD ? (nyq ? b.Xnyq : b.X) : (nyq ? b.Tnyq : b.T);
-  float R = 0.f, sc = 0.f;
-  int k2cut = 0;
-  if (OP == B_COL_Z_INV) { const RadB rd = b.rad[radius]; R = rd.R; k2cut = rd.k2cut; sc = b.growth * b.inv_n3; }
+  // z inverse: W depends on |k|^2 = kz^2 + (the column's ky^2 + kx^2), N/2 + 1 distinct values per
+  // column; they go into B (free until the transform) before the tile is loaded
+  float* wcol = reinterpret_cast<float*>(B);
+  if (OP == B_COL_Z_INV) {
+    const RadB rd = b.rad[radius];
+    const float sc = b.growth * b.inv_n3;
+    for (int q = threadIdx.x; q < TI * (M + 1); q += BT) {
+      const int col = q / (M + 1), kz = q % (M + 1);
+      const int ck2 = !nyq ? wrap2<N>(plane) + (c * TI + col) * (c * TI + col) : wrap2<N>(c * TI + col) + M * M;
+      wcol[q] = filter_weight(kz * kz + ck2, b.dk, rd.R, rd.k2cut, b.filter, b.ref_compat) * sc;
+    }
+    __syncthreads();
+  }
   for (int e = threadIdx.x; e < N * TI; e += BT) {
     const int row = e / TI, col = e % TI;
     float2 v = __ldcg(src + off + row * es_g + col);
-    if (OP == B_COL_Z_INV) {
-      int k2;
-      if (!nyq) { const int kx = c * TI + col; k2 = wrap2<N>(row) + wrap2<N>(plane) + kx * kx; }
-      else k2 = wrap2<N>(row) + wrap2<N>(c * TI + col) + M * M;
-      v = cscale(v, filter_weight(k2, b.dk, R, k2cut, b.filter, b.ref_compat) * sc);
-    }
+    if (OP == B_COL_Z_INV) v = cscale(v, wcol[col * (M + 1) + (row > M ? N - row : row)]);
     A[e] = v;
   }
   if (OP == B_COL_Y_INV && c == 0) {
