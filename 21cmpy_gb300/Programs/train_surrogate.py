@@ -1,7 +1,7 @@
 """Train and evaluate the learned surrogate on pairs generated by the plain engine.
 
     python -m 21cmpy_gb300.Programs.train_surrogate [--n 128] [--box-len 200] [--train 2048]
-        [--held 128] [--epochs 8] [--lr 3e-4] [--out weights.pt] [--report report.json]
+        [--held 128] [--epochs 12] [--lr 3e-4] [--decay 0.8] [--out weights.pt] [--report report.json]
     python -m 21cmpy_gb300.Programs.train_surrogate --conv-only [--n 128]
 
 Training pairs: Gaussian random fields of seeds 1000..(1000 + train - 1) at n^3 with parameter
@@ -30,8 +30,9 @@ def main(argv=None):
     ap.add_argument("--box-len", type=float, default=200.0)
     ap.add_argument("--train", type=int, default=2048)
     ap.add_argument("--held", type=int, default=128)
-    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--lr", type=float, default=3e-4)
+    ap.add_argument("--decay", type=float, default=0.8, help="step-size factor per epoch")
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
@@ -59,7 +60,7 @@ def main(argv=None):
     losses = []
     for ep in range(args.epochs):
         perm = order_rng.permutation(len(train))
-        losses.extend(S.train(net, [train[i] for i in perm], epochs=1, lr=args.lr * (0.7 ** ep),
+        losses.extend(S.train(net, [train[i] for i in perm], epochs=1, lr=args.lr * (args.decay ** ep),
                               log=lambda m, ep=ep: log(m.replace("epoch 0:", f"epoch {ep}:", 1))))
     torch.cuda.synchronize()
     t_train = time.time() - t0
@@ -73,22 +74,24 @@ def main(argv=None):
     st = S.schedule.ionize_setup(gen.n, gen.box_len, s.z, zeta=s.zeta, t_vir_min=s.t_vir, R_max=s.R_max,
                                  cosmo=gen.cosmo, table=gen.table)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(3):
-        net.forward(f)
-    e0.record()
-    for _ in range(10):
-        net.forward(f)
-    e1.record()
-    e1.synchronize()
-    sg_ms = e0.elapsed_time(e1) / 10
-    for _ in range(3):
-        gen.plan.run(s.delta, st)
-    e0.record()
-    for _ in range(10):
-        gen.plan.run(s.delta, st)
-    e1.record()
-    e1.synchronize()
-    eng_ms = e0.elapsed_time(e1) / 10
+
+    def best_ms(fn, rounds=3, reps=10):
+        """Fastest of a few timed rounds (both sides alike), after warm-up."""
+        for _ in range(3):
+            fn()
+        times = []
+        for _ in range(rounds):
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / reps)
+        return min(times)
+
+    sg_ms = best_ms(lambda: net.forward(f))
+    eng_ms = best_ms(lambda: gen.plan.run(s.delta, st))
+    from ..autotune import cached as tuned_config
     flop = 2 * gen.n ** 3 * sum(27 * ci * co for ci, co in S.LAYERS)
 
     sweep = S.SurrogateSweep(net, gen, max_abs_err=0.05, check_every=8)
@@ -100,7 +103,8 @@ def main(argv=None):
         "trained": trained, "untrained": untrained, "constant_mean_abs_dxHI": const_err,
         "surrogate_ms_per_box": sg_ms, "surrogate_boxes_per_s": 1e3 / sg_ms,
         "surrogate_tflops": flop / sg_ms / 1e9,
-        "engine_ms_per_box": eng_ms, "engine_boxes_per_s": 1e3 / eng_ms,
+        "engine_ms_per_box": eng_ms, "engine_boxes_per_s": 1e3 / eng_ms, "engine_radii": st.n_radii,
+        "engine_config": tuned_config(gen.plan.device, gen.n),
         "speed_ratio_surrogate_over_engine": eng_ms / sg_ms,
         "sweep": {"points": len(kinds), "surrogate": kinds.count("surrogate"), "engine": kinds.count("engine")},
     }
