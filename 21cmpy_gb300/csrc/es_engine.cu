@@ -528,6 +528,7 @@ int es_plan_create(int n, double box_len, int max_radii, es_plan** out) {
   es_plan* p = new es_plan();
   p->n = n; p->m = n / 2; p->box_len = box_len; p->max_radii = max_radii; p->size = se;
   p->k2n = 3 * p->m * p->m + 1;
+  p->hr.reserve(max_radii);         // es_ionize fills it without reallocating
   // DELTA_K = float32(2 pi / float32(BOX_LEN)) (delta_T.py:52)
   p->dk = (float)(2.0 * M_PI / (double)(float)box_len);
   se->geom(&p->geo);
