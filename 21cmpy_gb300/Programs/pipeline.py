@@ -47,6 +47,14 @@ def simulate_box(deltax, param_dict, Z=None, fil=0, update=0, LE=False, *, param
             "ps_ave": pk_h[0], "count": pk_h[2], "n_radii": setup.n_radii}
 
 
+def lane_slot(i: int, lanes: int):
+    """(lane, device slot) of box i when ``lanes`` boxes run side by side: box i runs on lane
+    i mod lanes, and each lane alternates between two slots, so a slot is reused by box i + 2 lanes
+    and never by a box that can still be in flight beside it."""
+    lane = i % lanes
+    return lane, 2 * lane + ((i // lanes) & 1)
+
+
 def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=None, num_bins=None,
                    ref_compat=False, xH_outs=None, dT_outs=None, device=None, lanes=3):
     """``simulate_box`` for many boxes of one size, with the copies overlapped with the compute and
@@ -106,8 +114,7 @@ def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=N
         ev_comp = [torch.cuda.Event() for _ in range(nbox)]
         ev_out = [torch.cuda.Event() for _ in range(nbox)]
         for i in range(nbox):
-            lane = i % K
-            slot = 2 * lane + ((i // K) & 1)                  # box i - 2K used this slot last
+            lane, slot = lane_slot(i, K)                      # box i - 2K used this slot last
             comp, plan = comps[lane], plans[lane]
             with torch.cuda.stream(s_in):
                 if i >= 2 * K:
