@@ -273,6 +273,7 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
       if (!t.nyq) { const int kx = t.c * TI + col; ck2 = wrap2<N>(t.plane) + kx * kx; wgt = kx == 0 ? 1.f : 2.f; }
       else { ck2 = wrap2<N>(t.c * TI + col) + M * M; wgt = 1.f; }
       int cur = -1;
+      int pos = -1;                                          // bin of the previous k in this run
       float ap = 0.f, ak = 0.f, an = 0.f;
       auto flush = [&](bool mine) {
         const int key = mine ? cur : -1;
@@ -295,8 +296,18 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
         const int k = k0 + q;
         const bool valid = k < N;
         const int k2 = wrap2<N>(valid ? k : 0) + ck2;
-        int lo = 0, hi = a.nbins;                            // first bin with k2 <= thr[bin]
-        while (lo < hi) { const int mid = (lo + hi) >> 1; if (k2 <= sthr[mid]) hi = mid; else lo = mid + 1; }
+        // first bin with k2 <= thr[bin]: a binary search for the run's first k, then a walk from the
+        // previous k's bin (|k|^2 rises, then falls past N/2, so the bin moves by a step or two)
+        int lo = pos;
+        if (lo < 0) {
+          int hi = a.nbins;
+          lo = 0;
+          while (lo < hi) { const int mid = (lo + hi) >> 1; if (k2 <= sthr[mid]) hi = mid; else lo = mid + 1; }
+        } else {
+          while (lo < a.nbins && k2 > sthr[lo]) ++lo;
+          while (lo > 0 && k2 <= sthr[lo - 1]) --lo;
+        }
+        pos = lo;
         const int bin = (k2 == 0 || !valid) ? a.nbins : lo;    // the mean (k = 0) is excluded
         const bool change = bin != cur;
         if (__any_sync(0xffffffffu, change && cur >= 0 && cur < a.nbins))
