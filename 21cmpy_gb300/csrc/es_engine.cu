@@ -754,19 +754,28 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     // while the row pass of radius r (caller's stream) runs.  Radius r + 1 writes the spectrum
     // that radius r - 1 read, so it waits for that row pass; each row pass waits for its own
     // column passes.  Everything the plan stream does is joined back before the last row pass.
+    // On a failed launch, whatever the plan stream holds is still joined to the caller's stream.
+    auto joined = [&](int code) {
+      if (cudaEventRecord(p->ev_fork, p->aux) == cudaSuccess) cudaStreamWaitEvent(s, p->ev_fork, 0);
+      return code;
+    };
     ES_CUDA(cudaEventRecord(p->ev_fork, s));
     ES_CUDA(cudaStreamWaitEvent(p->aux, p->ev_fork, 0));
-    if ((rc = col_passes(0, p->aux))) return rc;
-    ES_CUDA(cudaEventRecord(p->ev_col[0], p->aux));
+    if ((rc = col_passes(0, p->aux))) return joined(rc);
+    if (cudaEventRecord(p->ev_col[0], p->aux) != cudaSuccess) return joined(fail(ES_E_CUDA, "es_ionize: event record failed"));
     for (int r = 0; r < nr; ++r) {
       if (r + 1 < nr) {
-        if (r >= 1) ES_CUDA(cudaStreamWaitEvent(p->aux, p->ev_row[(r + 1) & 1], 0));
-        if ((rc = col_passes(r + 1, p->aux))) return rc;
-        ES_CUDA(cudaEventRecord(p->ev_col[(r + 1) & 1], p->aux));
+        if (r >= 1 && cudaStreamWaitEvent(p->aux, p->ev_row[(r + 1) & 1], 0) != cudaSuccess)
+          return joined(fail(ES_E_CUDA, "es_ionize: stream wait failed"));
+        if ((rc = col_passes(r + 1, p->aux))) return joined(rc);
+        if (cudaEventRecord(p->ev_col[(r + 1) & 1], p->aux) != cudaSuccess)
+          return joined(fail(ES_E_CUDA, "es_ionize: event record failed"));
       }
-      ES_CUDA(cudaStreamWaitEvent(s, p->ev_col[r & 1], 0));
-      if ((rc = row_pass(r))) return rc;
-      ES_CUDA(cudaEventRecord(p->ev_row[r & 1], s));
+      if (cudaStreamWaitEvent(s, p->ev_col[r & 1], 0) != cudaSuccess)
+        return joined(fail(ES_E_CUDA, "es_ionize: stream wait failed"));
+      if ((rc = row_pass(r))) return joined(rc);
+      if (cudaEventRecord(p->ev_row[r & 1], s) != cudaSuccess)
+        return joined(fail(ES_E_CUDA, "es_ionize: event record failed"));
     }
   }
   slot = prof_begin(p, ES_PROF_FINAL, s);
