@@ -69,15 +69,15 @@ def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=N
     boxes as torch CPU tensors; results are identical to box-by-box ``simulate_box``.
     """
     import torch
-    p = _common.params(params)
-    boxes = [b if isinstance(b, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(b, np.float32)).pin_memory()
-             for b in boxes]
+    if int(lanes) < 1:
+        raise ValueError("lanes must be >= 1")
     if len(boxes) != len(Zs):
         raise ValueError("one redshift per box")
     if not boxes:
         return []
-    if lanes < 1:
-        raise ValueError("lanes must be >= 1")
+    p = _common.params(params)
+    boxes = [b if isinstance(b, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(b, np.float32)).pin_memory()
+             for b in boxes]
     n = int(boxes[0].shape[0])
     if any(tuple(b.shape) != (n, n, n) or b.dtype != torch.float32 or b.is_cuda for b in boxes):
         raise ValueError("boxes must be host float32 (N, N, N) tensors or arrays of one size")

@@ -69,3 +69,15 @@ def test_bench_roofline_line():
     assert app["share_of_event_time"] == pytest.approx(0.4)
     assert app["launch_ms"] == pytest.approx(1e3 * 0.03 * 0.4 / 100)
     assert app["achieved"] == pytest.approx(b / (app["launch_ms"] / 1e3) / 1e9)
+
+
+def test_sweep_argument_checks_come_first():
+    # bad arguments are reported before any device work (here there is no device at all)
+    pipe = module("Programs.pipeline")
+    import numpy as np
+    box = np.zeros((8, 8, 8), np.float32)
+    with pytest.raises(ValueError, match="lanes"):
+        pipe.simulate_sweep([box], {"BoxSize": 12.0}, [8.0], lanes=0)
+    with pytest.raises(ValueError, match="redshift"):
+        pipe.simulate_sweep([box, box], {"BoxSize": 12.0}, [8.0])
+    assert pipe.simulate_sweep([], {"BoxSize": 12.0}, []) == []
