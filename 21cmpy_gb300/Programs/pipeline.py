@@ -47,6 +47,9 @@ def simulate_box(deltax, param_dict, Z=None, fil=0, update=0, LE=False, *, param
             "ps_ave": pk_h[0], "count": pk_h[2], "n_radii": setup.n_radii}
 
 
+MAX_LANES = 4
+
+
 def lane_slot(i: int, lanes: int):
     """(lane, device slot) of box i when ``lanes`` boxes run side by side: box i runs on lane
     i mod lanes, and each lane alternates between two slots, so a slot is reused by box i + 2 lanes
@@ -89,7 +92,9 @@ def simulate_sweep(boxes, param_dict, Zs, fil=0, update=0, LE=False, *, params=N
               for z in Zs]
     consts = [cosmology.brightness_temperature_factor(float(z), cosmo) for z in Zs]
     nbox = len(boxes)
-    K = min(int(lanes), nbox)
+    # at most MAX_LANES plans of a size: the plan cache must hold them all (four lanes measured no
+    # faster than three at 256^3)
+    K = min(int(lanes), nbox, MAX_LANES)
     radii = max(s.n_radii for s in setups)
     plans = [_common.plan_for(n, box_len, radii, device, lane=k) for k in range(K)]
     dev = plans[0].device

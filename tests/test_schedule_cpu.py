@@ -81,3 +81,10 @@ def test_sweep_argument_checks_come_first():
     with pytest.raises(ValueError, match="redshift"):
         pipe.simulate_sweep([box, box], {"BoxSize": 12.0}, [8.0])
     assert pipe.simulate_sweep([], {"BoxSize": 12.0}, []) == []
+
+
+def test_lane_plans_fit_the_plan_cache():
+    pipe = module("Programs.pipeline")
+    common = module("Programs._common")
+    # every lane of a sweep keeps its plan cached while a plan of another size stays cached too
+    assert common.MAX_CACHED_PLANS >= 2 * pipe.MAX_LANES
