@@ -46,6 +46,10 @@ def test_host_only_calls(lib):
     assert lib.es_plan_workspace_bytes(100, 10) == 0          # unsupported size
     w = lib.es_plan_workspace_bytes(256, 40)
     assert 300e6 < w < 500e6
+    # input spectrum, two intermediate spectra, two delta_R boxes, centre list, per-radius window
+    # tables: 420 MB at 256^3 and 3.3 GB at 512^3 with room for 64 radii
+    assert abs(lib.es_plan_workspace_bytes(256, 64) / 420e6 - 1) < 0.02
+    assert abs(lib.es_plan_workspace_bytes(512, 64) / 3.3e9 - 1) < 0.02
     lib.es_version.restype = C.c_int
     assert lib.es_version() >= 1
 
