@@ -13,6 +13,7 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libes_engine.so"
 
 ES_OK = 0
+ES_E_ARG, ES_E_CUDA, ES_E_NOMEM, ES_E_UNSUPPORTED, ES_E_DEVICE = -1, -2, -3, -4, -5
 # kernel kinds reported by es_profile_read (ES_PROF_* in include/es_engine.h)
 PROF_KINDS = ("col_z_fwd", "col_y_fwd", "col_z_inv_filter", "col_y_inv", "col_z_fwd_pk", "row_r2c",
               "row_r2c_pk", "row_c2r", "row_c2r_ionize", "col_z_inv", "filter_table", "final",
@@ -28,6 +29,11 @@ OPT_ROW_RADIX = 6
 OPT_OVERLAP = 7
 OPT_ROW_CTAS = 8
 OPT_COL_CTAS = 9
+OPT_WAIT_LOG2 = 10
+OPT_DEBUG_STALL = 11
+STALL_COL_Z_INV = 1
+STALL_ROW_C2R = 2
+STALL_ROW_R2C = 3
 
 
 class EngineUnavailable(RuntimeError):

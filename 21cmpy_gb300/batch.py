@@ -236,6 +236,26 @@ def boxes_from_specs(specs, device=None, cosmo=None, table=None):
     return out
 
 
+def box_cost(n: int, n_radii: int) -> int:
+    """Work of one box: N^3 voxels times its number of filter radii (each radius is one inverse
+    transform with the fcoll epilogue; the forward transform and the final step are per box)."""
+    return int(n) ** 3 * int(n_radii)
+
+
+def shard_specs(specs, world: int, cosmo=None):
+    """Splits BoxSpec work items over ranks by their cost N^3 * N_R (longest processing time first).
+
+    The radius count of every box comes from its own schedule (R_mfp, cell size), so boxes of the
+    same size with different R_mfp weigh differently.  Returns one list of spec indices per rank.
+    """
+    from .cosmology import BASELINE_COSMO
+    from .schedule import ionize_setup
+    cosmo = cosmo or BASELINE_COSMO
+    costs = [box_cost(s.n, ionize_setup(s.n, s.box_len, s.z, zeta=s.zeta, t_vir_min=s.t_vir_min,
+                                        R_max=s.R_max, cosmo=cosmo).n_radii) for s in specs]
+    return shard(costs, world)
+
+
 def shard(costs, world: int):
     """Longest-processing-time split of work items (cost per item) over `world` ranks.
 

@@ -121,6 +121,8 @@ struct es_plan {
   int l2_hints = 1;                 // keep the intermediate spectrum in L2 when it fits
   long l2_bytes = 0;                // device L2 size
   unsigned* err = nullptr;          // device error word (timed-out waits)
+  int wait_log2 = 0;                // ES_OPT_WAIT_LOG2 (0: the kernels' default limit)
+  int stall = 0;                    // ES_OPT_DEBUG_STALL: pass whose first tile of CTA 0 times out
 };
 
 namespace {
@@ -399,6 +401,7 @@ es::OpArgs base_args(const es_plan* p) {
   a.col_radix = p->col_radix;
   a.row_radix = p->row_radix;
   a.scale = 1.0f;
+  a.wait_log2 = p->wait_log2;
   return a;
 }
 
@@ -426,6 +429,9 @@ void prof_end(es_plan* p, int slot, cudaStream_t s) {
 
 int run_op(es_plan* p, int op, es::OpArgs a, int grid, cudaStream_t s) {
   a.grid = grid;
+  a.stall = (p->stall == ES_STALL_COL_Z_INV && op == es::OP_COL_Z_INV_FILTER) ||
+            (p->stall == ES_STALL_ROW_C2R && op == es::OP_ROW_C2R_IONIZE) ||
+            (p->stall == ES_STALL_ROW_R2C && op == es::OP_ROW_R2C_SCALE);
   const int slot = prof_begin(p, op, s);
   cudaError_t e = p->size->launch(op, &a, s);
   prof_end(p, slot, s);
@@ -960,6 +966,14 @@ int es_plan_set_option(es_plan* p, int option, int value) {
       if (value < 0 || value > 16) return fail(ES_E_ARG, "es_plan_set_option: CTAs per SM must be in [0, 16]");
       (option == ES_OPT_ROW_CTAS ? p->row_per_sm : p->col_per_sm) = value;
       return ES_OK;
+    case ES_OPT_WAIT_LOG2:
+      if (value != 0 && (value < 8 || value > 30)) return fail(ES_E_ARG, "es_plan_set_option: wait limit must be 0 or 8..30");
+      p->wait_log2 = value;
+      return ES_OK;
+    case ES_OPT_DEBUG_STALL:
+      if (value < 0 || value > ES_STALL_ROW_R2C) return fail(ES_E_ARG, "es_plan_set_option: unknown debug stall %d", value);
+      p->stall = value;
+      return ES_OK;
     default:
       return fail(ES_E_ARG, "es_plan_set_option: unknown option %d", option);
   }
@@ -977,6 +991,8 @@ int es_plan_get_option(es_plan* p, int option, int* value) {
     case ES_OPT_OVERLAP: *value = p->overlap; return ES_OK;
     case ES_OPT_ROW_CTAS: *value = p->row_per_sm; return ES_OK;
     case ES_OPT_COL_CTAS: *value = p->col_per_sm; return ES_OK;
+    case ES_OPT_WAIT_LOG2: *value = p->wait_log2; return ES_OK;
+    case ES_OPT_DEBUG_STALL: *value = p->stall; return ES_OK;
     default: return fail(ES_E_ARG, "es_plan_get_option: unknown option %d", option);
   }
 }

@@ -36,6 +36,8 @@ struct OpArgs {
   int hint_in, hint_out;          // L2 policies of the TMA loads / stores (ES_HINT_*)
   int discard_in;                 // row pass: drop the consumed input lines from L2
   int grid;                       // CTAs to launch (persistent grid-stride)
+  int wait_log2;                  // TMA passes: 2^wait_log2 mbarrier polls before a wait times out (0: default)
+  int stall;                      // TMA passes: debug stall of CTA 0's first tile (the wait times out)
   // real boxes viewed as float2 pairs of consecutive x
   const float2* rin;
   float2* rout;

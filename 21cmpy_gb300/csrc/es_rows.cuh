@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
   const uint64_t pol_in = l2_policy(a.hint_in), pol_prev = l2_policy(ES_HINT_EVICT_FIRST);
   auto issue = [&](int it, int s) {
     const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
-    mbar_expect_tx(&bars[s], has_prev ? 2 * tile_bytes : tile_bytes);
+    mbar_expect_tx(&bars[s], (has_prev ? 2 * tile_bytes : tile_bytes) + stall_bytes(a.stall, it));
     bulk_load(s ? S1 : S0, a.cin + pair0, tile_bytes, &bars[s], pol_in);
     if (has_prev) bulk_load(s ? P1 : P0, a.prev + pair0, tile_bytes, &bars[s], pol_prev);
   };
@@ -94,12 +94,15 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
   for (int it = 0; it < my_count; ++it) {
     const int s = it & 1;
     const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
-    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1))) {
+    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1), a.wait_log2)) {
       atomicOr(a.err, ES_DEV_ERR_TIMEOUT);
       s_abort = 1;
     }
     __syncthreads();
-    if (s_abort) break;
+    if (s_abort) {
+      if (threadIdx.x == 0) drain_tile_loads(bars, it, my_count, a.wait_log2);
+      break;
+    }
     // C2R split + transpose: Z[m] = (X[m] + conj X[M-m]) + i w^-m (X[m] - conj X[M-m]).  Item t of
     // row l makes Z[t] and Z[M-t]; item 0 makes Z[0] from the packed (X[0], X[N/2]) and the
     // self-paired Z[M/2].  RL * M/2 items: every thread has whole items, no division when M/2 is a
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_r2
   const uint32_t tile_bytes = RL * M * 8;
   auto issue = [&](int it, int s) {
     const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
-    mbar_expect_tx(&bars[s], tile_bytes);
+    mbar_expect_tx(&bars[s], tile_bytes + stall_bytes(a.stall, it));
     bulk_load(s ? S1 : S0, a.rin + pair0, tile_bytes, &bars[s], l2_policy(a.hint_in));
   };
   if (threadIdx.x == 0) {
@@ -238,12 +241,15 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_r2
   for (int it = 0; it < my_count; ++it) {
     const int s = it & 1;
     const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
-    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1))) {
+    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1), a.wait_log2)) {
       atomicOr(a.err, ES_DEV_ERR_TIMEOUT);
       s_abort = 1;
     }
     __syncthreads();
-    if (s_abort) break;
+    if (s_abort) {
+      if (threadIdx.x == 0) drain_tile_loads(bars, it, my_count, a.wait_log2);
+      break;
+    }
     const float2* src = s ? S1 : S0;
     for (int e = threadIdx.x; e < RL * M; e += T) {
       const int row = e / M, p = e % M;

@@ -8,7 +8,7 @@
 namespace es {
 
 constexpr unsigned ES_DEV_ERR_TIMEOUT = 1u;
-constexpr long kWaitLimit = 1L << 26;      // mbarrier polls before a wait is declared hung
+constexpr int kWaitLog2 = 26;             // default: 2^26 mbarrier polls before a wait is declared hung
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -29,10 +29,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long it = 0; it < kWaitLimit; ++it)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int wait_log2) {
+  const long limit = 1L << (wait_log2 > 0 ? wait_log2 : kWaitLog2);
+  for (long it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+// After a timed-out wait at tile `it`, the loads issued for tiles it and it + 1 (two in flight)
+// may still be landing in this CTA's shared memory.  Thread 0 waits for them, bounded like every
+// other wait, before the CTA leaves, so no copy outlives the CTA that owns its destination.
+__device__ __forceinline__ void drain_tile_loads(uint64_t* bars, int it, int count, int wait_log2) {
+  for (int j = it; j < it + 2 && j < count; ++j) mbar_wait(&bars[j & 1], (uint32_t)((j >> 1) & 1), wait_log2);
+}
+// Debug stall: CTA 0 announces 16 bytes more than its first tile brings, so that tile's wait can
+// only end by timing out (the copies themselves complete normally).
+__device__ __forceinline__ uint32_t stall_bytes(int stall, int it) {
+  return (stall && it == 0 && blockIdx.x == 0) ? 16u : 0u;
 }
 __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -132,11 +144,12 @@ __device__ __forceinline__ TileCoord tile_coord(int tile) {
 // Tile load: z-pass boxes are (TI, 1, BOX) at (c TI, j, k0); y-pass boxes (TI, BOX, 1) at (c TI, j0, k);
 // Nyquist-plane boxes (TI, BOX) at (c TI, k0).  BOX = min(N, 256) (a TMA box side is <= 256).
 template <int N, int MODE, int V>
-__device__ __forceinline__ void issue_tile_load(const OpArgs& a, const TileCoord& t, float2* dst, uint64_t* bar) {
+__device__ __forceinline__ void issue_tile_load(const OpArgs& a, const TileCoord& t, float2* dst, uint64_t* bar,
+                                                uint32_t extra = 0) {
   constexpr int TI = ColTile<N, V>::TI;
   constexpr int BOX = N < 256 ? N : 256;
   constexpr bool ZPASS = (MODE == COL_Z_FWD || MODE == COL_Z_INV_FILTER || MODE == COL_Z_FWD_PK || MODE == COL_Z_INV);
-  mbar_expect_tx(bar, (uint32_t)(N * TI * 8));
+  mbar_expect_tx(bar, (uint32_t)(N * TI * 8) + extra);
   const uint64_t pol = l2_policy(a.hint_in);
 #pragma unroll
   for (int h = 0; h < N / BOX; ++h) {
@@ -205,7 +218,8 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
     fence_mbar_init();
     fence_async_smem();
     for (int s = 0; s < 2 && s < my_count; ++s)
-      issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + s * gridDim.x), s ? S1 : S0, &bars[s]);
+      issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + s * gridDim.x), s ? S1 : S0, &bars[s],
+                                  stall_bytes(a.stall, s));
   }
   for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
   if (MODE == COL_Z_FWD_PK) {
@@ -229,12 +243,15 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
         wcol[q] = filter_weight(kz * kz + ck2, a.dk, a.fR, a.fk2cut, a.filter, a.ref_compat) * scale;
       }
     }
-    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1))) {
+    if (!mbar_wait(&bars[s], (uint32_t)((it >> 1) & 1), a.wait_log2)) {
       atomicOr(a.err, ES_DEV_ERR_TIMEOUT);
       s_abort = 1;
     }
     __syncthreads();
-    if (s_abort) break;
+    if (s_abort) {
+      if (threadIdx.x == 0) drain_tile_loads(bars, it, my_count, a.wait_log2);
+      break;
+    }
 
     float2* out;
     if (MODE == COL_Z_INV_FILTER) {

@@ -56,10 +56,13 @@ class BoxSpec:
     t_vir_min: float
 
 
-def sweep_256() -> list:
-    """HII_DIM=256, L=300 Mpc, seeds 0-3 x z = 6.0, 6.5, ..., 12.0; zeta=30, R_mfp=15, Tvir=1e4."""
+def sweep_256(seeds=range(4)) -> list:
+    """HII_DIM=256, L=300 Mpc, seeds 0-3 x z = 6.0, 6.5, ..., 12.0; zeta=30, R_mfp=15, Tvir=1e4.
+
+    ``seeds`` widens the sweep to more realisations of the same redshift grid (weak scaling over
+    several GPUs: 4 seeds per GPU)."""
     zs = [6.0 + 0.5 * i for i in range(13)]
-    return [BoxSpec(256, 300.0, s, z, 30.0, 15.0, 1.0e4) for s in range(4) for z in zs]
+    return [BoxSpec(256, 300.0, s, z, 30.0, 15.0, 1.0e4) for s in seeds for z in zs]
 
 
 def single_64() -> BoxSpec:

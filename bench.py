@@ -120,18 +120,33 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def make_workload(rank: int, boxes: int):
+def make_workload(rank: int, world: int, boxes: int):
+    """This rank's boxes: the sweep widened to 4 seeds per GPU, split over ranks by cost N^3 * N_R
+    (batch.shard_specs); with every box of equal cost each rank gets one full 52-box sweep."""
     grf = importlib.import_module("21cmpy_gb300.grf")
-    specs = grf.sweep_256()[:boxes]
-    # weak scaling: rank r takes seeds 4r..4r+3 of the same redshift grid
+    batch = importlib.import_module("21cmpy_gb300.batch")
+    specs = grf.sweep_256(seeds=range(4 * world))
+    mine = [specs[i] for i in batch.shard_specs(specs, world)[rank]][:boxes]
     base = {}
     out = []
-    for s in specs:
-        seed = s.seed + 4 * rank
-        if seed not in base:
-            base[seed] = grf.grf_z0(s.n, s.box_len, seed)
-        out.append((s, seed, grf.density_box(s.n, s.box_len, seed, s.z, base=base[seed])))
+    for s in mine:
+        if s.seed not in base:
+            base[s.seed] = grf.grf_z0(s.n, s.box_len, s.seed)
+        out.append((s, s.seed, grf.density_box(s.n, s.box_len, s.seed, s.z, base=base[s.seed])))
     return out
+
+
+def sweep_config(nboxes: int, radii_per_box: int, world: int) -> dict:
+    """The workload both arms report (the reference arm times a bounded sample of it)."""
+    return {"workload": f"excursion-set sweep: {nboxes} boxes of 256^3 per GPU (seeds 0-3 x z=6.0..12.0 step 0.5), "
+                        "BOX_LEN=300 Mpc, zeta=30, R_mfp=15 Mpc, Tvir=1e4 K, real-space top-hat, "
+                        f"{radii_per_box} radii/box, delta_T + {NUM_BINS}-bin P(k)",
+            "n": N, "box_len_mpc": BOX_LEN, "boxes_per_gpu": nboxes, "radii_per_box": radii_per_box,
+            "l2": "no flush: every box's inputs (64 MiB density + 64 MiB spectrum) and its 256 MiB working "
+                  "set exceed the 129 MB L2, and consecutive boxes touch different inputs",
+            "parallelism": f"{world} independent GPU(s), 4 seeds x 13 redshifts per GPU split by cost N^3 N_R "
+                           f"(batch.shard_specs), no collective; {LANES} boxes side by side per GPU "
+                           "(one plan and stream each)"}
 
 
 def setups_for(work):
@@ -145,50 +160,73 @@ def setups_for(work):
     return res
 
 
-def cpu_baseline(work, setups, radii: int) -> dict:
-    """FP64 numpy oracle (numpy.fft, one thread) on the first `radii` radii of one box."""
+def oracle_box(O, d, st, c, edges, backend="numpy", workers=1):
+    """One box of the sweep on the host: every radius, the final step, delta_T and P(k)."""
+    ion = O.conv_bubbles(d, st, backend=backend, workers=workers)["ionized"]
+    dT, ave = O.delta_T(1.0 - ion, d, c)
+    O.power_spectrum(dT, ave, BOX_LEN, edges, backend=backend, workers=workers)
+
+
+def cpu_baseline(work, setups) -> dict:
+    """FP64 numpy oracle (numpy.fft, one thread) on one whole box of the sweep."""
     from oracle import es_oracle as O
-    s, _seed, d = work[0]
-    st, _c = setups[0]
+    sch = importlib.import_module("21cmpy_gb300.schedule")
+    s, seed, d = work[0]
+    st, c = setups[0]
+    edges = sch.pk_edges(N, BOX_LEN, NUM_BINS)
     t0 = time.perf_counter()
-    O.conv_bubbles(d, st, max_radii=radii)
+    oracle_box(O, d, st, c, edges)
     dt = time.perf_counter() - t0
-    return {"value": N ** 3 * radii / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"one 256^3 box (seed {_seed}, z={s.z}), forward FFT + first {radii} of {st.n_radii} radii, "
-                      f"numpy.fft float64 single thread, {dt:.1f} s"}
+    return {"value": N ** 3 * st.n_radii / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"one whole 256^3 box of the sweep (seed {seed}, z={s.z}): forward FFT, all {st.n_radii} "
+                      f"radii, final step, delta_T and {NUM_BINS}-bin P(k); numpy.fft float64, one thread, {dt:.1f} s"}
 
 
 def run_reference(args):
     """Reference arm: the oracle port of the path on all host cores (scipy.fft workers and a thread
-    pool over slabs for the per-radius elementwise work)."""
+    pool over slabs for the per-radius elementwise work), one whole box of the sweep per step."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return 0
     from oracle import es_oracle as O
-    work = make_workload(0, 1)
+    sch = importlib.import_module("21cmpy_gb300.schedule")
+    # a few distinct boxes of rank 0's sweep, taken in turn (every box has the same radius count)
+    distinct = max(1, min(4, args.warmup + args.steps))
+    work = make_workload(0, world, distinct)
     setups = setups_for(work)
-    s, _seed, d = work[0]
-    st, _c = setups[0]
+    edges = sch.pk_edges(N, BOX_LEN, NUM_BINS)
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    radii = args.ref_radii
+    # the config of the GPU arm at the same world size: the full sweep's box and radius counts
+    grf = importlib.import_module("21cmpy_gb300.grf")
+    full = grf.sweep_256()[:args.boxes]
+    radii = setups[0][0].n_radii
+    config = sweep_config(len(full), radii, world)
+    count = [0]
 
     def step():
-        O.conv_bubbles(d, st, backend="scipy", workers=cores, max_radii=radii)
+        i = count[0] % len(work)
+        count[0] += 1
+        st, c = setups[i]
+        oracle_box(O, work[i][2], st, c, edges, backend="scipy", workers=cores)
+        return st.n_radii
 
     for _ in range(args.warmup):
         step()
     t0 = time.perf_counter()
+    updates = 0
     for _ in range(args.steps):
-        step()
+        updates += N ** 3 * step()
     dt = time.perf_counter() - t0
-    value = N ** 3 * radii * args.steps / dt
-    sample = (f"one 256^3 box per step (seed 0, z={s.z}), forward FFT + first {radii} of {st.n_radii} radii, "
-              f"float64, scipy.fft and the per-radius window / erfc / threshold slabs on {cores} threads")
+    value = updates / dt
+    sample = (f"one whole box of the {len(full)}-box sweep per step ({len(work)} distinct boxes taken in turn): "
+              f"forward FFT, all {radii} of {radii} radii, final step, delta_T and {NUM_BINS}-bin P(k); float64, "
+              f"scipy.fft and the per-radius window / erfc / threshold slabs on {cores} threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded BBKS Gaussian random fields)",
-            "config": {"workload": "excursion-set sweep 256^3 (bounded CPU sample)", "n": N, "box_len_mpc": BOX_LEN},
+            "data": "synthetic (seeded BBKS Gaussian random fields, Om=0.31 Ob=0.049 h=0.68 s8=0.81)",
+            "config": config,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -202,8 +240,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--boxes", type=int, default=52, help="boxes per step (the sweep has 52)")
-    ap.add_argument("--cpu-radii", type=int, default=6, help="radii in the timed CPU sample")
-    ap.add_argument("--ref-radii", type=int, default=4, help="radii per reference-arm step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven batched-sweep measurement")
@@ -233,7 +269,7 @@ def main():
     eng = importlib.import_module("21cmpy_gb300.engine")
     sch = importlib.import_module("21cmpy_gb300.schedule")
 
-    work = make_workload(rank, args.boxes)
+    work = make_workload(rank, world, args.boxes)
     setups = setups_for(work)
     edges = sch.pk_edges(N, BOX_LEN, NUM_BINS)
     nboxes = len(work)
@@ -378,14 +414,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded BBKS Gaussian random fields, Om=0.31 Ob=0.049 h=0.68 s8=0.81)",
-        "config": {"workload": f"excursion-set sweep: {nboxes} boxes of 256^3 per GPU (seeds 0-3 x z=6.0..12.0 step 0.5), "
-                               "BOX_LEN=300 Mpc, zeta=30, R_mfp=15 Mpc, Tvir=1e4 K, real-space top-hat, "
-                               f"{radii_total // nboxes} radii/box, delta_T + {NUM_BINS}-bin P(k)",
-                   "n": N, "box_len_mpc": BOX_LEN, "boxes_per_gpu": nboxes, "radii_per_box": radii_total // nboxes,
-                   "l2": "no flush: every box's inputs (64 MiB density + 64 MiB spectrum) and its 256 MiB working "
-                         "set exceed the 129 MB L2, and consecutive boxes touch different inputs",
-                   "parallelism": f"{world} independent GPU(s), boxes sharded by seed, no collective; "
-                                  f"{LANES} boxes side by side per GPU (one plan and stream each)"},
+        "config": sweep_config(nboxes, radii_total // nboxes, world),
         "gpu_launches": int(sum(c for _ms, c in prof.values())),
         "autotune": {"config": tuned.get("config"), "source": tuned.get("source"),
                      "meaning": "(pass variant, column tile, row tile, column radix schedule, row radix schedule, overlapped radii, row-pass CTAs per SM, column-pass CTAs per SM)"},
@@ -412,7 +441,7 @@ def main():
     if perturb_info is not None:
         line["perturb_field"] = perturb_info
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(work, setups, args.cpu_radii)
+        line["cpu_baseline"] = cpu_baseline(work, setups)
     if rank == 0:
         print(json.dumps(line), flush=True)
     for p_ in plans:

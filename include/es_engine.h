@@ -89,6 +89,19 @@ int es_supported_sizes(int* sizes, int cap);
 #define ES_OPT_OVERLAP 7
 #define ES_OPT_ROW_CTAS 8
 #define ES_OPT_COL_CTAS 9
+/* ES_OPT_WAIT_LOG2 (0 = default 26, else 8..30): a TMA pass gives up a wait on its tile after
+ * 2^value mbarrier polls, records the error word (es_plan_check) and leaves once the copies it
+ * issued have landed (a bounded wait too).
+ * ES_OPT_DEBUG_STALL (testing the failure path without a GPU fault): while set, CTA 0 of the
+ * chosen pass announces 16 bytes more than its first tile brings, so that wait can only time
+ * out: ES_STALL_COL_Z_INV (z inverse + filter of es_ionize), ES_STALL_ROW_C2R (row C2R +
+ * ionise), ES_STALL_ROW_R2C (row R2C of es_forward); 0 = off.  The results of a stalled call are
+ * invalid; the device stays usable. */
+#define ES_OPT_WAIT_LOG2 10
+#define ES_OPT_DEBUG_STALL 11
+#define ES_STALL_COL_Z_INV 1
+#define ES_STALL_ROW_C2R 2
+#define ES_STALL_ROW_R2C 3
 int es_plan_set_option(es_plan* plan, int option, int value);
 int es_plan_get_option(es_plan* plan, int option, int* value);
 /* Synchronises the stream and reports ES_E_DEVICE if any kernel of the plan gave up a bounded

@@ -2,14 +2,16 @@
 
 * ``sigma_kat.npz`` -- the reference's own sigma^2(R) tables (cosmo_files/sig0.npz and
   cosmo_files/Del2k.npz, produced by cosmo_files/sigmas.py:239-248 with cosmolopy): the full
-  Delta^2(k) table and every 10th radius of sig0.  Needs the reference checkout at
-  /root/reference (only this script reads it).
+  Delta^2(k) table and every 10th radius of sig0.  Needs a checkout of the reference: its
+  path comes from ``--reference DIR`` or the ``ES_REFERENCE_DIR`` environment variable (only
+  this script reads it); without one, this fixture is left as committed.
 * ``oracle_32.npz`` -- FP64 oracle outputs for seeded 32^3 boxes (centre and sphere modes,
   delta_T and P(k)), so the oracle itself is pinned against regressions and the GPU tests have
   a fixed target.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [--reference DIR]
 """
+import argparse
 import importlib
 import os
 import sys
@@ -19,12 +21,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference/cosmo_files"
 
 
-def sigma_kat():
-    a = np.load(os.path.join(REF, "sig0.npz"))
-    b = np.load(os.path.join(REF, "Del2k.npz"))
+def sigma_kat(ref_dir):
+    cosmo_files = os.path.join(ref_dir, "cosmo_files")
+    a = np.load(os.path.join(cosmo_files, "sig0.npz"))
+    b = np.load(os.path.join(cosmo_files, "Del2k.npz"))
     np.savez_compressed(os.path.join(HERE, "sigma_kat.npz"), k=b["k"], Del2=b["Del2"],
                         radius=a["radius"][::10], sig0=a["sig0"][::10], mass=a["mass"][::10])
 
@@ -56,7 +58,13 @@ def oracle_32():
 
 
 if __name__ == "__main__":
-    if os.path.isdir(REF):
-        sigma_kat()
+    ap = argparse.ArgumentParser(description="regenerate tests/golden fixtures")
+    ap.add_argument("--reference", default=os.environ.get("ES_REFERENCE_DIR"),
+                    help="checkout of the reference repository (for sigma_kat.npz)")
+    args = ap.parse_args()
+    if args.reference and os.path.isdir(os.path.join(args.reference, "cosmo_files")):
+        sigma_kat(args.reference)
+    else:
+        print("no reference checkout given (--reference / ES_REFERENCE_DIR): sigma_kat.npz left as committed")
     oracle_32()
     print("fixtures written to", HERE)

@@ -1,0 +1,136 @@
+"""Parity on the benchmark configurations themselves, against the FP64 oracle.
+
+* the 64^3 box exactly as configured (BOX_LEN 100 Mpc, seed 0, z 8, zeta 30, R_mfp 15 Mpc,
+  T_vir 1e4 K, real-space top hat): ionisation, delta_T and the 20-bin P(k);
+* one 512^3 box (BOX_LEN 600 Mpc, z 7.5, zeta 40, R_mfp 30 Mpc, 40 radii): ionisation, mean x_HI,
+  delta_T and P(k), the oracle on all host cores (scipy.fft workers);
+* sphere painting at 128^3 (find_bubbles.cu:73-140; radius R / cell in cells, periodic);
+* the uneven 64-box batch (HII_DIM ~ U{64, 96, 128, 160}): the plan-graph batch and the persistent
+  batched launch against per-box plans for every box, and the first 160^3 box against the oracle.
+
+Bars: parity_util (flags except within 1e-5 of the threshold, mean x_HI and P(k) to 1e-4).
+delta_T and P(k) are checked on the engine's own x_HI (the oracle computes them from the same
+x_HI), so the check isolates their arithmetic from the near-threshold flag band.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import module
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import es_oracle as O  # noqa: E402
+from parity_util import FLAG_TOL, PARTIAL_ATOL, compare_ionized, compare_pk  # noqa: E402
+
+cos = module("cosmology")
+sch = module("schedule")
+grf = module("grf")
+WORKERS = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module")
+def eng():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return module("engine")
+
+
+def _setup(spec, **kw):
+    return sch.ionize_setup(spec.n, spec.box_len, spec.z, zeta=spec.zeta, t_vir_min=spec.t_vir_min,
+                            R_max=spec.R_max, cosmo=cos.BASELINE_COSMO, **kw)
+
+
+def _box_chain(eng, spec, st, d, label, max_radii=64):
+    """Engine: ionisation, delta_T, P(k); oracle: the same on the engine's x_HI; both compared."""
+    n, L = spec.n, spec.box_len
+    c = cos.brightness_temperature_factor(spec.z, cos.BASELINE_COSMO)
+    edges = sch.pk_edges(n, L, 20)
+    with eng.ExcursionSetPlan(n, L, max_radii=max_radii) as p:
+        dd = torch.from_numpy(d).cuda()
+        ion, _ = p.run(dd, st, output="ionized")
+        ion_h = ion.cpu().numpy()
+        del ion
+        xh, nf = p.run(dd, st)
+        dT, ave = p.delta_T(xh, dd, c)
+        pk = p.power_spectrum(dT, ave, edges).cpu().numpy()
+        xh_h, dT_h, ave_h, nf_h = xh.cpu().numpy(), dT.cpu().numpy(), ave.item(), nf.item()
+        p.check()
+        del dd, xh, dT
+    torch.cuda.empty_cache()
+    assert np.array_equal(xh_h, np.float32(1.0) - ion_h), label
+    assert abs(nf_h - (1.0 - ion_h.mean(dtype=np.float64))) < 1e-5, label
+    dT_o, ave_o = O.delta_T(xh_h, d, c)
+    assert abs(ave_h - ave_o) <= 1e-5 * abs(ave_o), (label, ave_h, ave_o)
+    assert np.abs(dT_h - dT_o).max() <= 1e-5 * np.abs(dT_o).max(), label
+    compare_pk(pk, O.power_spectrum(dT_o, ave_o, L, edges, backend="scipy", workers=WORKERS), label)
+    return ion_h
+
+
+def test_config_64_box_exact(eng):
+    spec = grf.single_64()
+    assert (spec.n, spec.box_len, spec.seed, spec.z, spec.zeta, spec.R_max, spec.t_vir_min) == \
+        (64, 100.0, 0, 8.0, 30.0, 15.0, 1e4)
+    st = _setup(spec)
+    assert st.n_radii == 29 and st.filter_type == 0
+    d = grf.density_box(spec.n, spec.box_len, spec.seed, spec.z)
+    ref = O.conv_bubbles(d, st, tol=FLAG_TOL)
+    ion = _box_chain(eng, spec, st, d, "64^3 config")
+    compare_ionized(ion.astype(np.float64), ref, "64^3 config")
+
+
+@pytest.mark.skipif(os.environ.get("ES_SKIP_FULL") == "1", reason="full-size parity disabled")
+def test_config_512_box(eng):
+    spec = grf.single_512()
+    st = _setup(spec)
+    assert st.n_radii == 40
+    d = grf.density_box(spec.n, spec.box_len, spec.seed, spec.z)
+    ion = _box_chain(eng, spec, st, d, "512^3")
+    ref = O.conv_bubbles(d, st, tol=FLAG_TOL, backend="scipy", workers=WORKERS)
+    compare_ionized(ion.astype(np.float64), ref, "512^3")
+
+
+@pytest.mark.parametrize("ref_compat", [False])
+def test_sphere_painting_at_128(eng, ref_compat):
+    spec = grf.BoxSpec(128, 192.0, 31, 8.0, 30.0, 12.0, 1e4)
+    st = _setup(spec, update=1, ref_compat=ref_compat)
+    d = grf.density_box(spec.n, spec.box_len, spec.seed, spec.z)
+    ref = O.conv_bubbles(d, st, tol=FLAG_TOL)
+    with eng.ExcursionSetPlan(spec.n, spec.box_len) as p:
+        out, _ = p.run(torch.from_numpy(d).cuda(), st, output="ionized")
+    compare_ionized(out.cpu().numpy().astype(np.float64), ref, "sphere 128^3")
+    assert ref["flags"].mean() > 0.05           # the painting does real work here
+
+
+def test_uneven_64_box_batch(eng):
+    batch = module("batch")
+    specs = grf.uneven_batch()
+    assert len(specs) == 64 and {s.n for s in specs} == {64, 96, 128, 160}
+    boxes = batch.boxes_from_specs(specs)
+    per_box = []
+    for d, st in boxes:
+        with eng.ExcursionSetPlan(st.n, st.box_len) as p:
+            xh, nf = p.run(d, st)
+            per_box.append((xh.clone(), nf.item()))
+    # the plan graph (the form the benchmark reports): bit for bit the per-box plans
+    with batch.PlanGraphBatch(boxes, lanes=2, use_graph=True, tune=False) as g:
+        outs, nf = g.run()
+        g.check()
+        for i in range(len(boxes)):
+            assert torch.equal(outs[i], per_box[i][0]), i
+            assert nf[i].item() == per_box[i][1], i
+    # the persistent batched launch: same transforms, its own reduction order
+    with batch.BatchedExcursionSet(boxes, use_graph=True) as b:
+        outs, nf = b.run()
+        b.check()
+        for i in range(len(boxes)):
+            diff = (outs[i] - per_box[i][0]).abs()
+            assert (diff > PARTIAL_ATOL).float().mean().item() <= 1e-5, (i, diff.max().item())
+            assert abs(nf[i].item() - per_box[i][1]) <= 1e-5, i
+    # the first 160^3 box against the float64 oracle
+    i160 = next(i for i, s in enumerate(specs) if s.n == 160)
+    d, st = boxes[i160]
+    ref = O.conv_bubbles(d.cpu().numpy(), st, tol=FLAG_TOL, backend="scipy", workers=WORKERS)
+    compare_ionized(1.0 - per_box[i160][0].cpu().numpy().astype(np.float64), ref, "batch 160^3")

@@ -15,15 +15,11 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 from oracle import es_oracle as O  # noqa: E402
+from parity_util import FLAG_TOL, MEAN_RTOL, PARTIAL_ATOL, PK_RTOL, compare_ionized, compare_pk  # noqa: E402,F401
 
 cos = module("cosmology")
 sch = module("schedule")
 grf = module("grf")
-
-FLAG_TOL = 1e-5
-MEAN_RTOL = 1e-4
-PK_RTOL = 1e-4
-PARTIAL_ATOL = 2e-4
 
 
 @pytest.fixture(scope="module")
@@ -43,23 +39,7 @@ def _setup(n, L, z, **kw):
     return sch.ionize_setup(n, L, z, **base)
 
 
-def _compare_ionized(ion_gpu, ref, label=""):
-    """Every cell outside the oracle's exemption band must match the oracle's ionised fraction.
-
-    Loop radii decide flags (a flip there changes the cell from 1 to a partial value, far
-    beyond the tolerance); the final radius is continuous at the threshold (zeta f -> 1 from
-    below meets the flagged value 1), so it needs no exemption.
-    """
-    ion_o = ref["ionized"]
-    ex = ref["exempt"]
-    diff = np.abs(ion_gpu - ion_o)
-    bad = (diff > PARTIAL_ATOL) & ~ex
-    assert bad.sum() == 0, (f"{label}: {int(bad.sum())} cells differ by more than {PARTIAL_ATOL} outside "
-                            f"the {int(ex.sum())} exempt cells (max {diff[~ex].max():.3g})")
-    loop_flags = ref["flags"]
-    assert np.all(ion_gpu[loop_flags & ~ex] == 1.0), f"{label}: oracle-flagged cells not ionised"
-    xg, xo = 1.0 - ion_gpu.mean(), 1.0 - ion_o.mean()
-    assert abs(xg - xo) <= MEAN_RTOL * abs(xo) + 1e-7, f"{label}: mean x_HI {xg} vs {xo}"
+_compare_ionized = compare_ionized
 
 
 @pytest.mark.parametrize("n", [32, 48, 64, 96, 128, 160])
@@ -273,15 +253,29 @@ def test_power_spectrum_dimensional_and_ragged_bins(eng):
 
 @pytest.mark.skipif(os.environ.get("ES_SKIP_FULL") == "1", reason="full-size parity disabled")
 def test_full_size_256_box_matches_oracle(eng):
-    # one box of the 256^3 sweep, against the oracle run with multithreaded scipy.fft
+    # one box of the 256^3 sweep, against the oracle run with multithreaded scipy.fft: ionisation,
+    # then delta_T and the 20-bin P(k) of the engine's x_HI against the oracle's on the same x_HI
+    # (delta_T.py:73-98)
     b = grf.sweep_256()[5]
     d = grf.density_box(b.n, b.box_len, b.seed, b.z)
     st = _setup(b.n, b.box_len, b.z, zeta=b.zeta, R_max=b.R_max, t_vir_min=b.t_vir_min)
     assert st.n_radii == 32
     ref = O.conv_bubbles(d, st, tol=FLAG_TOL, backend="scipy", workers=os.cpu_count())
+    c = cos.brightness_temperature_factor(b.z, cos.BASELINE_COSMO)
+    edges = sch.pk_edges(b.n, b.box_len, 20)
     with _plan(eng, b.n, b.box_len) as p:
-        out, _ = p.run(torch.from_numpy(d).cuda(), st, output="ionized")
-    _compare_ionized(out.cpu().numpy().astype(np.float64), ref, "256^3")
+        dd = torch.from_numpy(d).cuda()
+        out, _ = p.run(dd, st, output="ionized")
+        ion = out.cpu().numpy().astype(np.float64)
+        xh, _ = p.run(dd, st)
+        dT, ave = p.delta_T(xh, dd, c)
+        pk = p.power_spectrum(dT, ave, edges).cpu().numpy()
+        xh_h, dT_h, ave_h = xh.cpu().numpy(), dT.cpu().numpy(), ave.item()
+    _compare_ionized(ion, ref, "256^3")
+    dT_o, ave_o = O.delta_T(xh_h, d, c)
+    assert abs(ave_h - ave_o) <= 1e-5 * abs(ave_o)
+    assert np.abs(dT_h - dT_o).max() <= 1e-5 * np.abs(dT_o).max()
+    compare_pk(pk, O.power_spectrum(dT_o, ave_o, b.box_len, edges, backend="scipy", workers=os.cpu_count()), "256^3")
 
 
 @pytest.mark.parametrize("update", [0, 1])
