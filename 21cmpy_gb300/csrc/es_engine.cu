@@ -305,7 +305,8 @@ __global__ void paint_kernel(const uint32_t* centers, const unsigned* count, uin
 
 __global__ void erfc_selftest_kernel(const float* x, float* fast, float* lib, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    fast[i] = es::erfc_sum_term(x[i]);
+    // the packed two-argument form the row pass uses (the second argument is a mirror image)
+    fast[i] = es::upk2(es::erfc_sum_pair(es::pk2(x[i], -x[i]))).x;
     lib[i] = erfcf(x[i]);
   }
 }

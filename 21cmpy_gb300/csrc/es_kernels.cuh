@@ -154,6 +154,78 @@ __device__ __forceinline__ float erfc_sum_term(float x) {
   return x >= 0.0f ? r : 2.0f - r;
 }
 
+// ------------------------------------------------------------ packed FP32 pairs (sm_100 and later)
+// A pair (lo, hi) of floats in one 64-bit register; fma/mul/add/sub.rn.f32x2 work on both halves
+// with one instruction.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ f32x2 bc2(float v) { return pk2(v, v); }
+__device__ __forceinline__ float2 upk2(f32x2 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// erfc_sum_term for two arguments at once on packed pairs (the same Numerical Recipes erfcc).
+// log2(e) is folded into the polynomial and the constant so the exponential is one ex2 of
+// (t P(t) - 1.26551223 - z^2) log2(e); z^2 = hi + lo is split exactly as above.  For x < 0 the
+// term is 2 - r, written as s r + (1 - s) with s = copysign(1, x) so both halves stay packed.
+__device__ __forceinline__ f32x2 erfc_sum_pair(f32x2 xv) {
+  constexpr float L2E = 1.4426950408889634f;
+  const float2 x = upk2(xv);
+  const float z0 = fabsf(x.x), z1 = fabsf(x.y);
+  const f32x2 Z = pk2(z0, z1), NZ = pk2(-z0, -z1);
+  const float2 d = upk2(fma2(Z, bc2(0.5f), bc2(1.0f)));
+  const f32x2 T = pk2(__fdividef(1.0f, d.x), __fdividef(1.0f, d.y));
+  f32x2 P = bc2(0.17087277f * L2E);
+  P = fma2(P, T, bc2(-0.82215223f * L2E));
+  P = fma2(P, T, bc2(1.48851587f * L2E));
+  P = fma2(P, T, bc2(-1.13520398f * L2E));
+  P = fma2(P, T, bc2(0.27886807f * L2E));
+  P = fma2(P, T, bc2(-0.18628806f * L2E));
+  P = fma2(P, T, bc2(0.09678418f * L2E));
+  P = fma2(P, T, bc2(0.37409196f * L2E));
+  P = fma2(P, T, bc2(1.00002368f * L2E));
+  const f32x2 H = mul2(Z, Z);                        // hi = z^2 rounded
+  const f32x2 NLO = fma2(NZ, Z, H);                  // hi - z^2 = -lo exactly
+  f32x2 E = fma2(T, P, bc2(-1.26551223f * L2E));
+  E = fma2(H, bc2(-L2E), E);
+  const float2 e = upk2(E);
+  f32x2 R = mul2(T, pk2(ex2_approx(e.x), ex2_approx(e.y)));
+  R = fma2(R, NLO, R);                               // r (1 - lo)
+  const f32x2 S = pk2(copysignf(1.0f, x.x), copysignf(1.0f, x.y));
+  return fma2(S, R, fma2(S, bc2(-1.0f), bc2(1.0f)));
+}
+
 // Real-space top-hat W(x) = 3 (sin x - x cos x) / x^3; below x = 1 its Taylor series
 // sum_n 3 (-1)^n (2n+2) x^(2n) / (2n+3)! avoids the cancellation of the closed form.  Above it the
 // hardware sine / cosine and division are used: for the arguments of a box (kR below ~150) their
@@ -193,6 +265,58 @@ __device__ __forceinline__ float filter_weight(int k2, float dk, float R, int k2
 template <int N> __device__ __forceinline__ int wrap2(int k) {
   const int w = (k > N / 2) ? k - N : k;
   return w * w;
+}
+
+// P(k) bins are kept per warp in shared memory as [3][PK_MAX_BINS]: the sums of k^3 |G|^2 / (2 pi^2 V)
+// and of |k| as float, and the mode counts (weights 1 or 2) as exact unsigned integers in the
+// third row (a bin of a 512^3 box holds more than 2^24 modes, beyond float32's exact integers).
+__device__ __forceinline__ unsigned* pk_counts(float* bins) { return reinterpret_cast<unsigned*>(bins) + 2 * PK_MAX_BINS; }
+
+// Per-CTA bins (fixed warp order) -> partials -> the last CTA to arrive adds the partials in a
+// fixed order and writes ps_ave, k_ave and the count (rounded to float32 once, at the end).
+template <int T>
+__device__ __forceinline__ void pk_finish(float* bins, const OpArgs& a) {
+  __syncthreads();
+  const int nb3 = 3 * a.nbins;
+  for (int idx = threadIdx.x; idx < nb3; idx += T) {
+    const int q = idx / a.nbins, bin = idx % a.nbins;
+    if (q < 2) {
+      float s = 0.f;
+      for (int w = 0; w < T / 32; ++w) s += bins[w * PK_MAX_BINS * 3 + q * PK_MAX_BINS + bin];
+      a.partials[(size_t)blockIdx.x * nb3 + idx] = s;
+    } else {
+      unsigned s = 0u;
+      for (int w = 0; w < T / 32; ++w) s += pk_counts(bins + w * PK_MAX_BINS * 3)[bin];
+      a.partials[(size_t)blockIdx.x * nb3 + idx] = __uint_as_float(s);
+    }
+  }
+  __shared__ unsigned s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  float* tot = bins;                                  // reuse: [3 * nbins]
+  for (int idx = threadIdx.x; idx < nb3; idx += T) {
+    if (idx < 2 * a.nbins) {
+      float s = 0.f;
+      for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(a.partials + (size_t)b * nb3 + idx);
+      tot[idx] = s;
+    } else {
+      unsigned long long s = 0ull;
+      for (int b = 0; b < (int)gridDim.x; ++b) s += __float_as_uint(__ldcg(a.partials + (size_t)b * nb3 + idx));
+      tot[idx] = __ull2float_rn(s);
+    }
+  }
+  __syncthreads();
+  for (int bin = threadIdx.x; bin < a.nbins; bin += T) {
+    const float n = tot[2 * a.nbins + bin];
+    a.pk_out[bin] = n > 0.f ? tot[bin] / n : 0.f;                        // ps_ave
+    a.pk_out[a.nbins + bin] = n > 0.f ? tot[a.nbins + bin] / n : 0.f;    // k_ave
+    a.pk_out[2 * a.nbins + bin] = n;                                     // count
+  }
+  if (threadIdx.x == 0) *a.counter = 0u;
 }
 
 // ------------------------------------------------------------------ column passes (y or z)
@@ -298,18 +422,19 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_pass(OpArgs a) {
         const float km = a.dk * sqrtf((float)k2);
         ws[lane * 4 + 0] = wgt * km * km * km * (g.x * g.x + g.y * g.y) * inv;
         ws[lane * 4 + 1] = wgt * km;
-        ws[lane * 4 + 2] = wgt;
+        reinterpret_cast<unsigned*>(ws)[lane * 4 + 2] = (unsigned)wgt;
         const unsigned peers = __match_any_sync(0xffffffffu, bin);
         __syncwarp();
         if (bin < a.nbins && lane == __ffs(peers) - 1) {
-          float p = 0.f, k = 0.f, n = 0.f;
+          float p = 0.f, k = 0.f;
+          unsigned n = 0u;
           unsigned m = peers;
           while (m) {
             const int l = __ffs(m) - 1;
             m &= m - 1;
-            p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += ws[l * 4 + 2];
+            p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += reinterpret_cast<const unsigned*>(ws)[l * 4 + 2];
           }
-          wb[bin] += p; wb[PK_MAX_BINS + bin] += k; wb[2 * PK_MAX_BINS + bin] += n;
+          wb[bin] += p; wb[PK_MAX_BINS + bin] += k; pk_counts(wb)[bin] += n;
         }
         __syncwarp();
       }
@@ -336,39 +461,7 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_pass(OpArgs a) {
     __syncthreads();
   }
 
-  if (MODE == COL_Z_FWD_PK) {
-    // per-CTA bins (fixed warp order) -> partials -> last CTA reduces and writes the averages
-    __syncthreads();
-    const int nb3 = 3 * a.nbins;
-    for (int idx = threadIdx.x; idx < nb3; idx += T) {
-      const int q = idx / a.nbins, bin = idx % a.nbins;
-      float s = 0.f;
-      for (int w = 0; w < T / 32; ++w) s += bins[w * PK_MAX_BINS * 3 + q * PK_MAX_BINS + bin];
-      a.partials[(size_t)blockIdx.x * nb3 + idx] = s;
-    }
-    __shared__ unsigned s_last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
-    __syncthreads();
-    if (s_last) {
-      __threadfence();
-      float* tot = bins;     // reuse: [3 * nbins]
-      for (int idx = threadIdx.x; idx < nb3; idx += T) {
-        float s = 0.f;
-        for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(a.partials + (size_t)b * nb3 + idx);
-        tot[idx] = s;
-      }
-      __syncthreads();
-      for (int bin = threadIdx.x; bin < a.nbins; bin += T) {
-        const float n = tot[2 * a.nbins + bin];
-        a.pk_out[bin] = n > 0.f ? tot[bin] / n : 0.f;                        // ps_ave
-        a.pk_out[a.nbins + bin] = n > 0.f ? tot[a.nbins + bin] / n : 0.f;    // k_ave
-        a.pk_out[2 * a.nbins + bin] = n;                                     // count
-      }
-      if (threadIdx.x == 0) *a.counter = 0u;
-    }
-  }
+  if (MODE == COL_Z_FWD_PK) pk_finish<T>(bins, a);
   (void)sred;
 }
 

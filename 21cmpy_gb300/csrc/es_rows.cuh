@@ -23,7 +23,8 @@ template <> struct Row2Cfg<512> { static constexpr int RL = 8,  T = 256; };
 template <int N, int V> struct RowTile {
   static constexpr int RL = V == 1 ? Row2Cfg<N>::RL / 2 : Row2Cfg<N>::RL;
   static constexpr int T = V == 0 ? Row2Cfg<N>::T : (V == 3 ? 2 * Row2Cfg<N>::T : Row2Cfg<N>::T / 2);
-  static constexpr int MINB = T >= 512 ? 2 : 1;
+  // two CTAs per SM: the shared memory of a tile allows it, and registers are capped to match
+  static constexpr int MINB = T >= 256 ? 2 : 1;
 };
 
 template <int N, bool PREV, int V> struct Row2Smem {
@@ -40,12 +41,63 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                : "memory");
 }
 
+// Stockham stages S.. STOP - 1 of a line FFT (line-fast thread mapping); returns the buffer that
+// holds the input of stage STOP.
+template <int N, int S, int STOP, bool INV, int NL, int T, int ES, int TWN, int RS, bool DONE = (S == STOP)>
+struct StagesTo {
+  static __device__ __forceinline__ float2* run(float2* a, float2* b, const float2* tw) {
+    stockham_stage<N, S, INV, NL, T, true, ES, 1, TWN, RS>(a, b, tw);
+    __syncthreads();
+    return StagesTo<N, S + 1, STOP, INV, NL, T, ES, TWN, RS>::run(b, a, tw);
+  }
+};
+template <int N, int S, int STOP, bool INV, int NL, int T, int ES, int TWN, int RS>
+struct StagesTo<N, S, STOP, INV, NL, T, ES, TWN, RS, true> {
+  static __device__ __forceinline__ float2* run(float2* a, float2*, const float2*) { return a; }
+};
+
+// The last Stockham stage of NL lines of length N held as [element][line] (pitch ES), with the
+// results handed to `out` in registers instead of written back.  Thread b takes butterfly
+// j = b % Ns of line l = b / Ns (consecutive threads: consecutive butterflies of one line), whose
+// outputs are the elements j + r Ns, r < R: for every r the threads of a line hold a run of Ns
+// consecutive elements.  out(l, j, v) receives the R outputs.
+template <int N, bool INV, int NL, int T, int ES, int TWN, int RS, class Out>
+__device__ __forceinline__ void last_stage_to_regs(const float2* __restrict__ in, const float2* __restrict__ tw, Out out) {
+  constexpr int S = Plan<N, RS>::stages - 1;
+  constexpr int R = Plan<N, RS>::radix[S];
+  constexpr int Ns = StageNs<N, S, RS>::value;
+  static_assert(Ns * R == N, "the last stage spans the line");
+  for (int b = threadIdx.x; b < NL * Ns; b += T) {
+    const int j = b % Ns, l = b / Ns;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = in[l + (j + r * Ns) * ES];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const float2 w = tw[j * r * (TWN / N)];
+        v[r] = twid<INV>(v[r], w.x, w.y);
+      }
+    }
+    Dft<R, INV>::run(v);
+    out(l, j, v);
+  }
+}
+
 // Half-spectrum rows -> real rows with the excursion-set epilogue (EPI_IONIZE) or a plain store.
 template <int N, int EPI, int V, int RS = 0>
 __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2r(const __grid_constant__ OpArgs a) {
   constexpr int M = N / 2, RL = RowTile<N, V>::RL, T = RowTile<N, V>::T, ES = RL + 1;
   constexpr bool PREV = EPI == EPI_IONIZE;
   using SM = Row2Smem<N, PREV, V>;
+  // last FFT stage: radix RLAST with NSL butterflies per line; its outputs go straight to the
+  // epilogue when every warp of it is full (ballots need whole warps)
+  constexpr int LAST = Plan<M, RS>::stages - 1;
+  constexpr int RLAST = Plan<M, RS>::radix[LAST];
+  constexpr int NSL = StageNs<M, LAST, RS>::value;
+  constexpr bool FUSED = (RL * NSL) % 32 == 0 && (NSL & (NSL - 1)) == 0;
+  constexpr int G = NSL < 32 ? NSL : 32;                 // lanes per run of consecutive pairs
+  constexpr unsigned GMASK = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
   static_assert((RL * N) % 64 == 0 && (RL * M) % 32 == 0, "row tiles must hold whole 64-voxel flag pairs");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -86,9 +138,10 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
     const float y = a.inv_zeta / a.stats_prev[2];
     if (y < 2.0f) thr_prev = a.dc - a.denom_prev * erfcinvf(y);
   }
-  const float dc = a.dc, inv_denom = PREV ? 1.0f / a.denom : 0.f;
+  const float inv_denom = PREV ? 1.0f / a.denom : 0.f;
+  const f32x2 DC = bc2(a.dc), INV = bc2(inv_denom);
   const int lane = threadIdx.x & 31;
-  float acc = 0.f;
+  f32x2 acc = bc2(0.0f);                              // two running sums (even, odd voxels)
   __syncthreads();
 
   for (int it = 0; it < my_count; ++it) {
@@ -132,52 +185,114 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
       for (int l = threadIdx.x; l < (int)(tile_bytes / 128); l += T) l2_discard(g + 128 * l);
     }
     __syncthreads();
-    float2* Zr = fft_lines<M, true, RL, T, true, ES, 1, N, RS>(A, B, tw);
-    if (EPI == EPI_STORE) {
-      for (int e = threadIdx.x; e < RL * M; e += T) {
-        const int row = e / M, p = e % M;
-        a.rout[pair0 + e] = Zr[p * ES + row];
+    if constexpr (FUSED) {
+      // all stages but the last in shared memory; the last one hands its outputs to the
+      // epilogue in registers (element p = j + r Ns of line l)
+      const float2* Y = StagesTo<M, 0, LAST, true, RL, T, ES, N, RS>::run(A, B, tw);
+      if (EPI == EPI_STORE) {
+        last_stage_to_regs<M, true, RL, T, ES, N, RS>(Y, tw, [&](int l, int j, const float2* v) {
+#pragma unroll
+          for (int r = 0; r < RLAST; ++r) a.rout[pair0 + (size_t)l * M + j + r * NSL] = v[r];
+        });
+      } else {
+        const float2* pv = s ? P1 : P0;
+        // one instantiation per (previous radius present, update mode): tests that are uniform
+        // over the launch stay out of the loop body
+        auto epilogue = [&](auto hp, auto upd) {
+          constexpr bool HP = decltype(hp)::value;
+          constexpr int UPD = decltype(upd)::value;
+          last_stage_to_regs<M, true, RL, T, ES, N, RS>(Y, tw, [&](int l, int j, const float2* v) {
+            const size_t row0 = pair0 + (size_t)l * M;
+#pragma unroll
+            for (int r = 0; r < RLAST; ++r) {
+              const int p = j + r * NSL;
+              const float2 d = v[r];
+              acc = add2(acc, erfc_sum_pair(mul2(sub2(DC, pk2(d.x, d.y)), INV)));
+              if (HP) {
+                const float2 pp = pv[l * M + p];
+                const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
+                const unsigned bx = __ballot_sync(0xffffffffu, px);
+                const unsigned by = __ballot_sync(0xffffffffu, py);
+                if (UPD == 0) {
+                  // pair-major bitmap: one 64-bit word per 32 pairs, even voxels in the low half.
+                  // The G lanes of a run hold G consecutive pairs starting at a multiple of G, so
+                  // the run lies in one word; its first lane ORs the run's bits in (fire and forget)
+                  const unsigned gx = (bx >> (lane & ~(G - 1))) & GMASK;
+                  const unsigned gy = (by >> (lane & ~(G - 1))) & GMASK;
+                  if ((lane & (G - 1)) == 0 && (gx | gy)) {
+                    const size_t pr = row0 + p;
+                    const int off = (int)(pr & 31);
+                    atomicOr(reinterpret_cast<unsigned long long*>(a.flags) + pr / 32,
+                             ((unsigned long long)gy << (32 + off)) | ((unsigned long long)gx << off));
+                  }
+                } else if (bx | by) {
+                  const unsigned cnt = __popc(bx) + __popc(by);
+                  unsigned first = 0;
+                  if (lane == 0) first = atomicAdd(a.center_count, cnt);
+                  first = __shfl_sync(0xffffffffu, first, 0);
+                  const unsigned lt = (1u << lane) - 1u;
+                  const unsigned v0 = (unsigned)((row0 + p) * 2);
+                  unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
+                  if (px) a.centers[pos++] = v0;
+                  if (py) a.centers[pos] = v0 + 1;
+                }
+              }
+              __stcs(a.rout + row0 + p, d);              // streamed: read again only next radius
+            }
+          });
+        };
+        if (!has_prev) epilogue(std::false_type{}, std::integral_constant<int, 0>{});
+        else if (a.update == 0) epilogue(std::true_type{}, std::integral_constant<int, 0>{});
+        else epilogue(std::true_type{}, std::integral_constant<int, 1>{});
       }
     } else {
-      const float2* pv = s ? P1 : P0;
-      // one loop per (previous radius present, update mode): tests that are uniform over the
-      // launch stay out of the loop body
-      auto epilogue = [&](auto hp, auto upd) {
-        constexpr bool HP = decltype(hp)::value;
-        constexpr int UPD = decltype(upd)::value;
-        for (int e = threadIdx.x; e < RL * M; e += T) {     // whole warps: 64 consecutive voxels
+      float2* Zr = fft_lines<M, true, RL, T, true, ES, 1, N, RS>(A, B, tw);
+      if (EPI == EPI_STORE) {
+        for (int e = threadIdx.x; e < RL * M; e += T) {
           const int row = e / M, p = e % M;
-          const float2 d = Zr[p * ES + row];
-          acc += erfc_sum_term((dc - d.x) * inv_denom) + erfc_sum_term((dc - d.y) * inv_denom);
-          if (HP) {
-            const float2 pp = pv[e];
-            const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
-            const unsigned bx = __ballot_sync(0xffffffffu, px);
-            const unsigned by = __ballot_sync(0xffffffffu, py);
-            if (UPD == 0) {
-              // pair-major bitmap: one 64-bit word per 32 pairs, even voxels in the low half;
-              // a fire-and-forget OR, so nothing on the warp's path waits for memory
-              if (lane == 0 && (bx | by))
-                atomicOr(reinterpret_cast<unsigned long long*>(a.flags) + (pair0 + e) / 32,
-                         ((unsigned long long)by << 32) | bx);
-            } else if (bx | by) {
-              const unsigned cnt = __popc(bx) + __popc(by);
-              unsigned first = 0;
-              if (lane == 0) first = atomicAdd(a.center_count, cnt);
-              first = __shfl_sync(0xffffffffu, first, 0);
-              const unsigned lt = (1u << lane) - 1u;
-              const unsigned v0 = (unsigned)((pair0 + e) * 2);
-              unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
-              if (px) a.centers[pos++] = v0;
-              if (py) a.centers[pos] = v0 + 1;
-            }
-          }
-          __stcs(a.rout + pair0 + e, d);                 // streamed: read again only next radius
+          a.rout[pair0 + e] = Zr[p * ES + row];
         }
-      };
-      if (!has_prev) epilogue(std::false_type{}, std::integral_constant<int, 0>{});
-      else if (a.update == 0) epilogue(std::true_type{}, std::integral_constant<int, 0>{});
-      else epilogue(std::true_type{}, std::integral_constant<int, 1>{});
+      } else {
+        const float2* pv = s ? P1 : P0;
+        // one loop per (previous radius present, update mode): tests that are uniform over the
+        // launch stay out of the loop body
+        auto epilogue = [&](auto hp, auto upd) {
+          constexpr bool HP = decltype(hp)::value;
+          constexpr int UPD = decltype(upd)::value;
+          for (int e = threadIdx.x; e < RL * M; e += T) {     // whole warps: 64 consecutive voxels
+            const int row = e / M, p = e % M;
+            const float2 d = Zr[p * ES + row];
+            acc = add2(acc, erfc_sum_pair(mul2(sub2(DC, pk2(d.x, d.y)), INV)));
+            if (HP) {
+              const float2 pp = pv[e];
+              const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
+              const unsigned bx = __ballot_sync(0xffffffffu, px);
+              const unsigned by = __ballot_sync(0xffffffffu, py);
+              if (UPD == 0) {
+                // pair-major bitmap: one 64-bit word per 32 pairs, even voxels in the low half;
+                // a fire-and-forget OR, so nothing on the warp's path waits for memory
+                if (lane == 0 && (bx | by))
+                  atomicOr(reinterpret_cast<unsigned long long*>(a.flags) + (pair0 + e) / 32,
+                           ((unsigned long long)by << 32) | bx);
+              } else if (bx | by) {
+                const unsigned cnt = __popc(bx) + __popc(by);
+                unsigned first = 0;
+                if (lane == 0) first = atomicAdd(a.center_count, cnt);
+                first = __shfl_sync(0xffffffffu, first, 0);
+                const unsigned lt = (1u << lane) - 1u;
+                const unsigned v0 = (unsigned)((pair0 + e) * 2);
+                unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
+                if (px) a.centers[pos++] = v0;
+                if (py) a.centers[pos] = v0 + 1;
+              }
+            }
+            __stcs(a.rout + pair0 + e, d);                 // streamed: read again only next radius
+          }
+        };
+        if (!has_prev) epilogue(std::false_type{}, std::integral_constant<int, 0>{});
+        else if (a.update == 0) epilogue(std::true_type{}, std::integral_constant<int, 0>{});
+        else epilogue(std::true_type{}, std::integral_constant<int, 1>{});
+      }
     }
     __syncthreads();                                   // S[s], P[s], A, B free again
     if (threadIdx.x == 0 && it + 2 < my_count) {
@@ -187,7 +302,8 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
   }
   if (EPI == EPI_IONIZE) {
     float total;
-    if (grid_sum<T>(acc, a.partials, a.counter, sred, &total) && threadIdx.x == 0) {
+    const float2 acc2 = upk2(acc);
+    if (grid_sum<T>(acc2.x + acc2.y, a.partials, a.counter, sred, &total) && threadIdx.x == 0) {
       const float mean = total / ((float)N * (float)N * (float)N);
       a.stats_out[0] = total;
       a.stats_out[1] = mean;

@@ -291,21 +291,24 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
       else { ck2 = wrap2<N>(t.c * TI + col) + M * M; wgt = 1.f; }
       int cur = -1;
       int pos = -1;                                          // bin of the previous k in this run
-      float ap = 0.f, ak = 0.f, an = 0.f;
+      float ap = 0.f, ak = 0.f;
+      unsigned an = 0u;                                      // mode count: exact integer
+      const unsigned wgt_u = (unsigned)wgt;
       auto flush = [&](bool mine) {
         const int key = mine ? cur : -1;
         const unsigned peers = __match_any_sync(0xffffffffu, key);
-        ws[lane * 4 + 0] = ap; ws[lane * 4 + 1] = ak; ws[lane * 4 + 2] = an;
+        ws[lane * 4 + 0] = ap; ws[lane * 4 + 1] = ak; reinterpret_cast<unsigned*>(ws)[lane * 4 + 2] = an;
         __syncwarp();
         if (mine && lane == __ffs(peers) - 1) {
-          float p = 0.f, k = 0.f, n = 0.f;
+          float p = 0.f, k = 0.f;
+          unsigned n = 0u;
           unsigned m = peers;
           while (m) {
             const int l = __ffs(m) - 1;
             m &= m - 1;
-            p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += ws[l * 4 + 2];
+            p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += reinterpret_cast<const unsigned*>(ws)[l * 4 + 2];
           }
-          wb[cur] += p; wb[PK_MAX_BINS + cur] += k; wb[2 * PK_MAX_BINS + cur] += n;
+          wb[cur] += p; wb[PK_MAX_BINS + cur] += k; pk_counts(wb)[cur] += n;
         }
         __syncwarp();
       };
@@ -329,13 +332,13 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
         const bool change = bin != cur;
         if (__any_sync(0xffffffffu, change && cur >= 0 && cur < a.nbins))
           flush(change && cur >= 0 && cur < a.nbins);
-        if (change) { cur = bin; ap = ak = an = 0.f; }
+        if (change) { cur = bin; ap = ak = 0.f; an = 0u; }
         if (!valid) continue;
         const float2 g = out[k * TI + col];
         const float km = a.dk * sqrtf((float)k2);
         ap += wgt * km * km * km * (g.x * g.x + g.y * g.y) * inv;
         ak += wgt * km;
-        an += wgt;
+        an += wgt_u;
       }
       flush(cur >= 0 && cur < a.nbins);
       __syncthreads();
@@ -379,38 +382,7 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
   }
   if (threadIdx.x == 0) bulk_wait0();
 
-  if (MODE == COL_Z_FWD_PK) {
-    __syncthreads();
-    const int nb3 = 3 * a.nbins;
-    for (int idx = threadIdx.x; idx < nb3; idx += T) {
-      const int q = idx / a.nbins, bin = idx % a.nbins;
-      float s = 0.f;
-      for (int w = 0; w < T / 32; ++w) s += bins[w * PK_MAX_BINS * 3 + q * PK_MAX_BINS + bin];
-      a.partials[(size_t)blockIdx.x * nb3 + idx] = s;
-    }
-    __shared__ unsigned s_last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(a.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
-    __syncthreads();
-    if (s_last) {
-      __threadfence();
-      float* tot = bins;
-      for (int idx = threadIdx.x; idx < nb3; idx += T) {
-        float s = 0.f;
-        for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(a.partials + (size_t)b * nb3 + idx);
-        tot[idx] = s;
-      }
-      __syncthreads();
-      for (int bin = threadIdx.x; bin < a.nbins; bin += T) {
-        const float n = tot[2 * a.nbins + bin];
-        a.pk_out[bin] = n > 0.f ? tot[bin] / n : 0.f;
-        a.pk_out[a.nbins + bin] = n > 0.f ? tot[a.nbins + bin] / n : 0.f;
-        a.pk_out[2 * a.nbins + bin] = n;
-      }
-      if (threadIdx.x == 0) *a.counter = 0u;
-    }
-  }
+  if (MODE == COL_Z_FWD_PK) pk_finish<T>(bins, a);
 }
 
 }  // namespace es
