@@ -194,29 +194,36 @@ __global__ void filter_table_kernel(float* wtab, int k2n, const RadDev* rad, int
   }
 }
 
+// Final radius (find_bubbles.cu:142-158): cells flagged at a loop radius stay ionised, the others
+// take zeta f, or 1 where f >= 1/zeta.  The flags come from the bitmap or, with `marker`, from
+// the lowest mantissa bit of the final delta_R (centre mode of the TMA row pass).  f uses the same
+// erfcc as the per-radius sums (relative error ~1e-7; the result is continuous at the threshold).
 template <int T>
-__global__ void __launch_bounds__(T) final_kernel(const float2* dR, const uint32_t* flags, long pairs,
+__global__ void __launch_bounds__(T) final_kernel(const float2* dR, const uint32_t* flags, int marker, long pairs,
                                                   float dc, float denom, const float* stats,
                                                   float zeta, float inv_zeta, int output,
                                                   float2* out, float* partials, unsigned* counter,
                                                   float* nf, float inv_n3) {
   __shared__ float sred[T / 32];
-  const float norm = stats[2];
+  const es::f32x2 NORM = es::bc2(stats[2]), DC = es::bc2(dc), INV = es::bc2(1.0f / denom);
   float acc = 0.f;
   for (long p = blockIdx.x * (long)T + threadIdx.x; p < pairs; p += (long)gridDim.x * T) {
     const float2 d = dR[p];
-    const unsigned long long w = __ldg(reinterpret_cast<const unsigned long long*>(flags) + p / 32);
-    const int bit = (int)(p % 32);
-    float ion[2];
-    const float dv[2] = {d.x, d.y};
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      if ((w >> (bit + 32 * h)) & 1ull) { ion[h] = 1.0f; continue; }
-      const float f = erfcf((dc - dv[h]) / denom) * norm;
-      ion[h] = f >= inv_zeta ? 1.0f : f * zeta;        // final_kernel (find_bubbles.cu:150-157)
+    unsigned fx, fy;
+    if (marker) {
+      fx = __float_as_uint(d.x) & 1u;
+      fy = __float_as_uint(d.y) & 1u;
+    } else {
+      const unsigned long long w = __ldg(reinterpret_cast<const unsigned long long*>(flags) + p / 32);
+      const int bit = (int)(p % 32);
+      fx = (unsigned)(w >> bit) & 1u;
+      fy = (unsigned)(w >> (bit + 32)) & 1u;
     }
-    acc += (1.0f - ion[0]) + (1.0f - ion[1]);
-    out[p] = output == 0 ? make_float2(1.0f - ion[0], 1.0f - ion[1]) : make_float2(ion[0], ion[1]);
+    const float2 f = es::upk2(es::mul2(es::erfc_sum_pair(es::mul2(es::sub2(DC, es::pk2(d.x, d.y)), INV)), NORM));
+    const float ix = fx ? 1.0f : (f.x >= inv_zeta ? 1.0f : f.x * zeta);
+    const float iy = fy ? 1.0f : (f.y >= inv_zeta ? 1.0f : f.y * zeta);
+    acc += (1.0f - ix) + (1.0f - iy);
+    out[p] = output == 0 ? make_float2(1.0f - ix, 1.0f - iy) : make_float2(ix, iy);
   }
   float total;
   if (es::grid_sum<T>(acc, partials, counter, sred, &total) && threadIdx.x == 0) *nf = total * inv_n3;
@@ -679,7 +686,10 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     ES_CUDA(cudaGetLastError());
   }
   const size_t N3 = (size_t)p->n * p->n * p->n;
-  ES_CUDA(cudaMemsetAsync(p->flags, 0, N3 / 8, s));
+  // centre mode on the TMA row pass carries the flags in delta_R itself; the bitmap serves the
+  // synchronous row pass and sphere painting
+  const int marker = (p->col_variant == 1 && prm->update == 0) ? 1 : 0;
+  if (!marker) ES_CUDA(cudaMemsetAsync(p->flags, 0, N3 / 8, s));
   const float inv_zeta = (float)(1.0 / (double)prm->zeta);
   // The intermediate spectrum T is written by the z pass, rewritten by the y pass and read by the
   // row pass; when it fits comfortably in L2 it is kept there (evict_last) while the input
@@ -737,6 +747,7 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
     a.stats_out = p->stats + (size_t)r * kStatsStride;
     a.inv_zeta = inv_zeta;
     a.update = prm->update;
+    a.marker = marker;
     a.centers = p->centers;
     a.center_count = p->counters + 1;
     a.fc_mean = prm->fc_mean_ps;
@@ -787,7 +798,7 @@ int es_ionize(es_plan* p, const es_ionize_params* prm, float* out, float* nf, vo
   }
   slot = prof_begin(p, ES_PROF_FINAL, s);
   final_kernel<256><<<grid_elem(p), 256, 0, s>>>(
-      reinterpret_cast<const float2*>(p->dR[(nr - 1) & 1]), p->flags, (long)(N3 / 2), prm->delta_c,
+      reinterpret_cast<const float2*>(p->dR[(nr - 1) & 1]), p->flags, marker, (long)(N3 / 2), prm->delta_c,
       prm->radii[nr - 1].denom, p->stats + (size_t)(nr - 1) * kStatsStride, prm->zeta, inv_zeta,
       prm->output, reinterpret_cast<float2*>(out), p->partials, p->counters, nf, inv_n3);
   prof_end(p, slot, s);

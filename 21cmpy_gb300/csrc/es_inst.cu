@@ -11,11 +11,13 @@
 
 namespace es {
 
-// One static flag per kernel (the template argument is the kernel itself): opt in to more than
-// 48 KB of dynamic shared memory once per kernel and device.
+// One static record per kernel (the template argument is the kernel itself) and device: opt in to
+// more than 48 KB of dynamic shared memory once, and remember how many CTAs of it fit on the
+// device at once (registers included), so a persistent grid never exceeds one resident wave.
 template <auto Kernel>
 static cudaError_t launch(int smem, const OpArgs& a, int threads, cudaStream_t s) {
   static unsigned configured = 0u;
+  static int resident[32];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -23,9 +25,16 @@ static cudaError_t launch(int smem, const OpArgs& a, int threads, cudaStream_t s
   if (!(configured & bit)) {
     e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, threads, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    resident[dev & 31] = (per_sm > 0 ? per_sm : 1) * sms;
     configured |= bit;
   }
-  Kernel<<<a.grid, threads, smem, s>>>(a);
+  const int grid = a.grid < resident[dev & 31] ? a.grid : resident[dev & 31];
+  Kernel<<<grid, threads, smem, s>>>(a);
   return cudaGetLastError();
 }
 

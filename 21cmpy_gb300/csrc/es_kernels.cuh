@@ -69,6 +69,8 @@ struct OpArgs {
   const float* stats_prev;        // {sum, mean, norm} of the previous radius
   float inv_zeta;                 // float32(1/zeta)
   int update;                     // 0 centre pixel, 1 sphere painting
+  int marker;                     // centre pixel: carry the flag in delta_R's lowest mantissa bit
+                                  // instead of the bitmap (TMA row pass)
   uint32_t* centers;              // sphere mode: centres passing at the previous radius
   unsigned* center_count;
   // reductions

@@ -23,16 +23,25 @@ template <> struct Row2Cfg<512> { static constexpr int RL = 8,  T = 256; };
 template <int N, int V> struct RowTile {
   static constexpr int RL = V == 1 ? Row2Cfg<N>::RL / 2 : Row2Cfg<N>::RL;
   static constexpr int T = V == 0 ? Row2Cfg<N>::T : (V == 3 ? 2 * Row2Cfg<N>::T : Row2Cfg<N>::T / 2);
-  // two CTAs per SM: the shared memory of a tile allows it, and registers are capped to match
-  static constexpr int MINB = T >= 256 ? 2 : 1;
 };
 
 template <int N, bool PREV, int V> struct Row2Smem {
   static constexpr int RL = RowTile<N, V>::RL, M = N / 2;
   static constexpr int stage = RL * M * 8;                 // one tile of rows, as loaded
   static constexpr int work = M * (RL + 1) * 8;            // transposed, padded
-  // [S0 | S1 | P0 | P1 | A | B | twiddles | mbarriers] after aligning the base to 128 bytes
-  static constexpr int bytes = (PREV ? 4 : 2) * stage + 2 * work + N * 8 + 16 + 128;
+  // [S0 | S1 | A | B | twiddles | 4 mbarriers] after aligning the base to 128 bytes.  With the
+  // ionisation epilogue the previous radius' tile lands in S[s] once the split has read the
+  // spectrum there, so it needs no buffers of its own.
+  static constexpr int bytes = 2 * stage + 2 * work + N * 8 + 32 + 128;
+};
+
+// Resident CTAs per SM that the shared memory of a row tile allows (227 KB per SM, 1 KB reserved
+// per CTA) and the threads (2048 per SM); registers are capped to match (__launch_bounds__).
+template <int N, int V> struct RowOcc {
+  static constexpr int by_smem = (227 * 1024) / (Row2Smem<N, true, V>::bytes + 1024);
+  static constexpr int by_threads = 2048 / RowTile<N, V>::T;
+  static constexpr int m = by_smem < by_threads ? by_smem : by_threads;
+  static constexpr int MINB = m < 1 ? 1 : (m > 8 ? 8 : m);
 };
 
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol) {
@@ -86,7 +95,7 @@ __device__ __forceinline__ void last_stage_to_regs(const float2* __restrict__ in
 
 // Half-spectrum rows -> real rows with the excursion-set epilogue (EPI_IONIZE) or a plain store.
 template <int N, int EPI, int V, int RS = 0>
-__global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2r(const __grid_constant__ OpArgs a) {
+__global__ void __launch_bounds__(RowTile<N, V>::T, RowOcc<N, V>::MINB) row2_c2r(const __grid_constant__ OpArgs a) {
   constexpr int M = N / 2, RL = RowTile<N, V>::RL, T = RowTile<N, V>::T, ES = RL + 1;
   constexpr bool PREV = EPI == EPI_IONIZE;
   using SM = Row2Smem<N, PREV, V>;
@@ -103,12 +112,10 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   float2* const S0 = reinterpret_cast<float2*>(base);
   float2* const S1 = reinterpret_cast<float2*>(base + SM::stage);
-  float2* const P0 = reinterpret_cast<float2*>(base + 2 * SM::stage);
-  float2* const P1 = reinterpret_cast<float2*>(base + 3 * SM::stage);
-  float2* A = reinterpret_cast<float2*>(base + (PREV ? 4 : 2) * SM::stage);
+  float2* A = reinterpret_cast<float2*>(base + 2 * SM::stage);
   float2* B = A + M * ES;
   float2* tw = B + M * ES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + N);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tw + N);     // [0, 1] spectrum tiles, [2, 3] previous radius
   __shared__ float sred[T / 32];
   __shared__ int s_abort;
 
@@ -119,14 +126,18 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
   const uint64_t pol_in = l2_policy(a.hint_in), pol_prev = l2_policy(ES_HINT_EVICT_FIRST);
   auto issue = [&](int it, int s) {
     const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
-    mbar_expect_tx(&bars[s], (has_prev ? 2 * tile_bytes : tile_bytes) + stall_bytes(a.stall, it));
+    mbar_expect_tx(&bars[s], tile_bytes + stall_bytes(a.stall, it));
     bulk_load(s ? S1 : S0, a.cin + pair0, tile_bytes, &bars[s], pol_in);
-    if (has_prev) bulk_load(s ? P1 : P0, a.prev + pair0, tile_bytes, &bars[s], pol_prev);
+  };
+  // delta_R of the previous radius for tile `it`, into the stage its spectrum has left
+  auto issue_prev = [&](int it, int s) {
+    const size_t pair0 = (size_t)(blockIdx.x + it * gridDim.x) * RL * M;
+    mbar_expect_tx(&bars[2 + s], tile_bytes);
+    bulk_load(s ? S1 : S0, a.prev + pair0, tile_bytes, &bars[2 + s], pol_prev);
   };
   if (threadIdx.x == 0) {
     s_abort = 0;
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    for (int b = 0; b < 4; ++b) mbar_init(&bars[b], 1);
     fence_mbar_init();
     fence_async_smem();
     for (int s = 0; s < 2 && s < my_count; ++s) issue(s, s);
@@ -184,7 +195,20 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
       const char* g = reinterpret_cast<const char*>(a.cin + pair0);
       for (int l = threadIdx.x; l < (int)(tile_bytes / 128); l += T) l2_discard(g + 128 * l);
     }
-    __syncthreads();
+    __syncthreads();                                   // the split has read S[s]
+    if (has_prev && threadIdx.x == 0) {
+      fence_async_smem();
+      issue_prev(it, s);
+    }
+    // every thread waits for the previous radius' tile before its epilogue reads it; a timeout
+    // marks the CTA, which finishes the tile (on stale data) and leaves at the end of it
+    auto wait_prev = [&]() {
+      if (has_prev && !mbar_wait(&bars[2 + s], (uint32_t)((it >> 1) & 1), a.wait_log2)) {
+        atomicOr(a.err, ES_DEV_ERR_TIMEOUT);
+        s_abort = 1;
+      }
+    };
+    const float2* pv = s ? S1 : S0;                    // the previous radius' tile, row-major
     if constexpr (FUSED) {
       // all stages but the last in shared memory; the last one hands its outputs to the
       // epilogue in registers (element p = j + r Ns of line l)
@@ -195,7 +219,6 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
           for (int r = 0; r < RLAST; ++r) a.rout[pair0 + (size_t)l * M + j + r * NSL] = v[r];
         });
       } else {
-        const float2* pv = s ? P1 : P0;
         // one instantiation per (previous radius present, update mode): tests that are uniform
         // over the launch stay out of the loop body
         auto epilogue = [&](auto hp, auto upd) {
@@ -203,12 +226,40 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
           constexpr int UPD = decltype(upd)::value;
           last_stage_to_regs<M, true, RL, T, ES, N, RS>(Y, tw, [&](int l, int j, const float2* v) {
             const size_t row0 = pair0 + (size_t)l * M;
+            // the erfc sum first: the RLAST chains are independent and overlap
+            f32x2 e[RLAST];
 #pragma unroll
-            for (int r = 0; r < RLAST; ++r) {
-              const int p = j + r * NSL;
-              const float2 d = v[r];
-              acc = add2(acc, erfc_sum_pair(mul2(sub2(DC, pk2(d.x, d.y)), INV)));
-              if (HP) {
+            for (int r = 0; r < RLAST; ++r) e[r] = erfc_sum_pair(mul2(sub2(DC, pk2(v[r].x, v[r].y)), INV));
+#pragma unroll
+            for (int r = 0; r < RLAST; ++r) acc = add2(acc, e[r]);
+            if (UPD == 2) {
+              // centre mode: whether a cell passed at an earlier radius travels in the lowest
+              // mantissa bit of delta_R (a change of at most one unit in the last place), so the
+              // next radius carries it forward with no bitmap and no atomics
+              if (HP) wait_prev();
+#pragma unroll
+              for (int r = 0; r < RLAST; ++r) {
+                const int p = j + r * NSL;
+                unsigned fx = 0u, fy = 0u;
+                if (HP) {
+                  const float2 pp = pv[l * M + p];
+                  fx = (__float_as_uint(pp.x) & 1u) | (pp.x >= thr_prev ? 1u : 0u);
+                  fy = (__float_as_uint(pp.y) & 1u) | (pp.y >= thr_prev ? 1u : 0u);
+                }
+                __stcs(a.rout + row0 + p, make_float2(__uint_as_float((__float_as_uint(v[r].x) & ~1u) | fx),
+                                                      __uint_as_float((__float_as_uint(v[r].y) & ~1u) | fy)));
+              }
+              return;
+            }
+#pragma unroll
+            for (int r = 0; r < RLAST; ++r)
+              __stcs(a.rout + row0 + j + r * NSL, v[r]);  // streamed: read again only next radius
+            if (HP) {
+              // then the previous radius' test on its tile, which has had all of the above to land
+              wait_prev();
+#pragma unroll
+              for (int r = 0; r < RLAST; ++r) {
+                const int p = j + r * NSL;
                 const float2 pp = pv[l * M + p];
                 const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
                 const unsigned bx = __ballot_sync(0xffffffffu, px);
@@ -237,23 +288,27 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
                   if (py) a.centers[pos] = v0 + 1;
                 }
               }
-              __stcs(a.rout + row0 + p, d);              // streamed: read again only next radius
             }
           });
         };
-        if (!has_prev) epilogue(std::false_type{}, std::integral_constant<int, 0>{});
-        else if (a.update == 0) epilogue(std::true_type{}, std::integral_constant<int, 0>{});
-        else epilogue(std::true_type{}, std::integral_constant<int, 1>{});
+        // update modes: 0 centre pixel with the bitmap, 1 sphere painting (centre list),
+        // 2 centre pixel with the flag carried in delta_R
+        if (!has_prev) {
+          if (a.marker) epilogue(std::false_type{}, std::integral_constant<int, 2>{});
+          else epilogue(std::false_type{}, std::integral_constant<int, 0>{});
+        } else if (a.update == 1) epilogue(std::true_type{}, std::integral_constant<int, 1>{});
+        else if (a.marker) epilogue(std::true_type{}, std::integral_constant<int, 2>{});
+        else epilogue(std::true_type{}, std::integral_constant<int, 0>{});
       }
     } else {
       float2* Zr = fft_lines<M, true, RL, T, true, ES, 1, N, RS>(A, B, tw);
+      wait_prev();
       if (EPI == EPI_STORE) {
         for (int e = threadIdx.x; e < RL * M; e += T) {
           const int row = e / M, p = e % M;
           a.rout[pair0 + e] = Zr[p * ES + row];
         }
       } else {
-        const float2* pv = s ? P1 : P0;
         // one loop per (previous radius present, update mode): tests that are uniform over the
         // launch stay out of the loop body
         auto epilogue = [&](auto hp, auto upd) {
@@ -263,6 +318,17 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
             const int row = e / M, p = e % M;
             const float2 d = Zr[p * ES + row];
             acc = add2(acc, erfc_sum_pair(mul2(sub2(DC, pk2(d.x, d.y)), INV)));
+            if (UPD == 2) {                                 // flag carried in delta_R (as above)
+              unsigned fx = 0u, fy = 0u;
+              if (HP) {
+                const float2 pp = pv[e];
+                fx = (__float_as_uint(pp.x) & 1u) | (pp.x >= thr_prev ? 1u : 0u);
+                fy = (__float_as_uint(pp.y) & 1u) | (pp.y >= thr_prev ? 1u : 0u);
+              }
+              __stcs(a.rout + pair0 + e, make_float2(__uint_as_float((__float_as_uint(d.x) & ~1u) | fx),
+                                                     __uint_as_float((__float_as_uint(d.y) & ~1u) | fy)));
+              continue;
+            }
             if (HP) {
               const float2 pp = pv[e];
               const bool px = pp.x >= thr_prev, py = pp.y >= thr_prev;
@@ -289,12 +355,23 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
             __stcs(a.rout + pair0 + e, d);                 // streamed: read again only next radius
           }
         };
-        if (!has_prev) epilogue(std::false_type{}, std::integral_constant<int, 0>{});
-        else if (a.update == 0) epilogue(std::true_type{}, std::integral_constant<int, 0>{});
-        else epilogue(std::true_type{}, std::integral_constant<int, 1>{});
+        if (!has_prev) {
+          if (a.marker) epilogue(std::false_type{}, std::integral_constant<int, 2>{});
+          else epilogue(std::false_type{}, std::integral_constant<int, 0>{});
+        } else if (a.update == 1) epilogue(std::true_type{}, std::integral_constant<int, 1>{});
+        else if (a.marker) epilogue(std::true_type{}, std::integral_constant<int, 2>{});
+        else epilogue(std::true_type{}, std::integral_constant<int, 0>{});
       }
     }
-    __syncthreads();                                   // S[s], P[s], A, B free again
+    __syncthreads();                                   // S[s], A, B free again
+    if (s_abort) {
+      // the previous radius' tile of this tile and the spectrum of the next may still be landing
+      if (threadIdx.x == 0) {
+        if (has_prev) mbar_wait(&bars[2 + s], (uint32_t)((it >> 1) & 1), a.wait_log2);
+        if (it + 1 < my_count) mbar_wait(&bars[s ^ 1], (uint32_t)(((it + 1) >> 1) & 1), a.wait_log2);
+      }
+      break;
+    }
     if (threadIdx.x == 0 && it + 2 < my_count) {
       fence_async_smem();
       issue(it + 2, s);
@@ -314,7 +391,7 @@ __global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_c2
 
 // Real rows -> half-spectrum rows (slot 0 holds (X[0], X[N/2])), with a scale or P(k) prologue.
 template <int N, int PRO, int V>
-__global__ void __launch_bounds__(RowTile<N, V>::T, RowTile<N, V>::MINB) row2_r2c(const __grid_constant__ OpArgs a) {
+__global__ void __launch_bounds__(RowTile<N, V>::T, RowOcc<N, V>::MINB) row2_r2c(const __grid_constant__ OpArgs a) {
   constexpr int M = N / 2, RL = RowTile<N, V>::RL, T = RowTile<N, V>::T, ES = RL + 1;
   using SM = Row2Smem<N, false, V>;
   extern __shared__ __align__(128) unsigned char smem_raw[];

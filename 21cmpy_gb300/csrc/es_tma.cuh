@@ -232,6 +232,18 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
     const int s = it & 1;
     float2* S = s ? S1 : S0;
     const TileCoord t = tile_coord<N, MODE, V>(blockIdx.x + it * gridDim.x);
+    if (threadIdx.x == 0 && it >= 1) {
+      // The store of tile it - 1 must have read its result out of shared memory before that
+      // buffer (or W) is written again; waiting here, beside the tile wait below, keeps the rest
+      // of the CTA from idling at a barrier behind it.  Tile it + 1 then goes into the buffer
+      // tile it - 1 arrived in.
+      bulk_wait_read0();
+      if (it + 1 < my_count) {
+        fence_async_smem();
+        issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + (it + 1) * gridDim.x), s ? S0 : S1,
+                                    &bars[s ^ 1]);
+      }
+    }
     if (MODE == COL_Z_INV_FILTER) {
       // W depends on |k|^2 = kz^2 + (ky^2 + kx^2 of the column): N/2 + 1 distinct values per
       // column.  Computed before waiting for the tile, so the arithmetic overlaps the copy.
@@ -371,14 +383,6 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
       __syncthreads();
       if (threadIdx.x == 0) issue_tile_store<N, MODE, V>(a, t, out);
     }
-    if (threadIdx.x == 0 && it + 2 < my_count) {
-      bulk_wait_read0();                  // the store above has finished reading shared memory
-      fence_async_smem();
-      issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + (it + 2) * gridDim.x), S, &bars[s]);
-    } else if (threadIdx.x == 0) {
-      bulk_wait_read0();
-    }
-    __syncthreads();
   }
   if (threadIdx.x == 0) bulk_wait0();
 

@@ -45,11 +45,13 @@ def kernel_bytes_per_voxel() -> dict:
     return {
         "col_z_inv_filter": 2 * HALF,                 # read spectrum, write filtered intermediate
         "col_y_inv": 2 * HALF,                        # read + write intermediate
-        "row_c2r_ionize": HALF + 4 + 4 + 2 * 0.125,   # read spectrum, write delta_R, read previous delta_R, flag bits r+w
+        # read spectrum, write delta_R, read previous delta_R; in centre mode the flags travel in
+        # delta_R's lowest mantissa bit, so no bitmap is read or written
+        "row_c2r_ionize": HALF + 4 + 4,
         "row_r2c": 4 + HALF,
         "col_y_fwd": 2 * HALF,
         "col_z_fwd": 2 * HALF,
-        "final": 4 + 0.125 + 4,
+        "final": 4 + 4,                               # read final delta_R (flags in it), write x_HI
         "delta_T": 12.0,
         "row_r2c_pk": 4 + HALF,
         "col_z_fwd_pk": HALF,
@@ -240,6 +242,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--boxes", type=int, default=52, help="boxes per step (the sweep has 52)")
+    ap.add_argument("--plan-config", default=None,
+                    help="apply this plan configuration (8 comma-separated integers, the autotuner's "
+                         "tuple) instead of tuning: makes a profiled run's launch sequence fixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the uneven batched-sweep measurement")
@@ -281,7 +286,14 @@ def main():
     pk = torch.empty((nboxes, 3, NUM_BINS), dtype=torch.float32, device=dev)
     at = importlib.import_module("21cmpy_gb300.autotune")
     plan = eng.ExcursionSetPlan(N, BOX_LEN, max_radii=64, device=dev)
-    tuned = at.ensure_tuned(plan)
+    if args.plan_config:
+        cfg = tuple(int(v) for v in args.plan_config.split(","))
+        if len(cfg) != 8:
+            ap.error("--plan-config needs 8 integers")
+        at.apply(plan, cfg)
+        tuned = {"config": list(cfg), "source": "given"}
+    else:
+        tuned = at.ensure_tuned(plan)
     # boxes are independent: LANES plans, each on its own stream, take boxes in turn
     plans = [plan] + [eng.ExcursionSetPlan(N, BOX_LEN, max_radii=64, device=dev) for _ in range(LANES - 1)]
     for p_ in plans[1:]:
