@@ -141,6 +141,46 @@ __device__ __forceinline__ TileCoord tile_coord(int tile) {
   return t;
 }
 
+// The tiles one CTA takes, in order.  Plain passes: tiles blockIdx.x + k gridDim.x.  The z inverse +
+// filter pass: first its share of the mirror-plane pairs (planes j and N - j of one column block,
+// back to back: the same |k|^2 column by column, so the filter weights of the first serve the
+// second), then its share of the remaining tiles (planes 0 and N/2, and the Nyquist plane).
+template <int N, int MODE, int V> struct TileSeq {
+  static constexpr int TI = ColTile<N, V>::TI, CPR = (N / 2) / TI;
+  static constexpr bool PAIRS = MODE == COL_Z_INV_FILTER;
+  static constexpr int NPAIR = PAIRS ? (N / 2 - 1) * CPR : 0;     // pair units
+  static constexpr int NREST = PAIRS ? 2 * CPR + N / TI : 0;      // single tiles after them
+  int npair_mine = 0, count = 0;
+  __device__ __forceinline__ explicit TileSeq(int ntiles) {
+    const int b = blockIdx.x, G = gridDim.x;
+    if (PAIRS) {
+      npair_mine = b < NPAIR ? (NPAIR - 1 - b) / G + 1 : 0;
+      count = 2 * npair_mine + (b < NREST ? (NREST - 1 - b) / G + 1 : 0);
+    } else {
+      count = b < ntiles ? (ntiles - 1 - b) / G + 1 : 0;
+    }
+  }
+  // the it-th tile; *reuse: the filter weights of the previous tile apply unchanged
+  __device__ __forceinline__ TileCoord at(int it, bool* reuse) const {
+    *reuse = false;
+    if (!PAIRS) return tile_coord<N, MODE, V>(blockIdx.x + it * gridDim.x);
+    TileCoord t;
+    t.nyq = false;
+    if (it < 2 * npair_mine) {
+      const int unit = blockIdx.x + (it >> 1) * gridDim.x;
+      const int jj = unit / CPR + 1;
+      t.c = unit % CPR;
+      t.plane = (it & 1) ? N - jj : jj;
+      *reuse = (it & 1) != 0;
+      return t;
+    }
+    const int k = blockIdx.x + (it - 2 * npair_mine) * gridDim.x;
+    if (k < 2 * CPR) { t.plane = k < CPR ? 0 : N / 2; t.c = k % CPR; }
+    else { t.nyq = true; t.plane = 0; t.c = k - 2 * CPR; }
+    return t;
+  }
+};
+
 // Tile load: z-pass boxes are (TI, 1, BOX) at (c TI, j, k0); y-pass boxes (TI, BOX, 1) at (c TI, j0, k);
 // Nyquist-plane boxes (TI, BOX) at (c TI, k0).  BOX = min(N, 256) (a TMA box side is <= 256).
 template <int N, int MODE, int V>
@@ -210,7 +250,9 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + 3 * TmaSmem<N, MODE, V>::tile + N * 8 + TmaSmem<N, MODE, V>::pk);
   __shared__ int s_abort;
 
-  const int my_count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const TileSeq<N, MODE, V> seq(ntiles);
+  const int my_count = seq.count;
+  bool reuse_w;
   if (threadIdx.x == 0) {
     s_abort = 0;
     mbar_init(&bars[0], 1);
@@ -218,8 +260,7 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
     fence_mbar_init();
     fence_async_smem();
     for (int s = 0; s < 2 && s < my_count; ++s)
-      issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + s * gridDim.x), s ? S1 : S0, &bars[s],
-                                  stall_bytes(a.stall, s));
+      issue_tile_load<N, MODE, V>(a, seq.at(s, &reuse_w), s ? S1 : S0, &bars[s], stall_bytes(a.stall, s));
   }
   for (int i = threadIdx.x; i < N; i += T) tw[i] = a.tw[i];
   if (MODE == COL_Z_FWD_PK) {
@@ -231,7 +272,7 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
   for (int it = 0; it < my_count; ++it) {
     const int s = it & 1;
     float2* S = s ? S1 : S0;
-    const TileCoord t = tile_coord<N, MODE, V>(blockIdx.x + it * gridDim.x);
+    const TileCoord t = seq.at(it, &reuse_w);
     if (threadIdx.x == 0 && it >= 1) {
       // The store of tile it - 1 must have read its result out of shared memory before that
       // buffer (or W) is written again; waiting here, beside the tile wait below, keeps the rest
@@ -240,13 +281,14 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
       bulk_wait_read0();
       if (it + 1 < my_count) {
         fence_async_smem();
-        issue_tile_load<N, MODE, V>(a, tile_coord<N, MODE, V>(blockIdx.x + (it + 1) * gridDim.x), s ? S0 : S1,
-                                    &bars[s ^ 1]);
+        bool unused;
+        issue_tile_load<N, MODE, V>(a, seq.at(it + 1, &unused), s ? S0 : S1, &bars[s ^ 1]);
       }
     }
-    if (MODE == COL_Z_INV_FILTER) {
+    if (MODE == COL_Z_INV_FILTER && !reuse_w) {
       // W depends on |k|^2 = kz^2 + (ky^2 + kx^2 of the column): N/2 + 1 distinct values per
-      // column.  Computed before waiting for the tile, so the arithmetic overlaps the copy.
+      // column.  Computed before waiting for the tile, so the arithmetic overlaps the copy; the
+      // mirror plane N - j that follows plane j uses the same values.
       const float scale = a.scale * a.inv_n3;
       for (int q = threadIdx.x; q < TI * (M + 1); q += T) {
         const int col = q / (M + 1), kz = q % (M + 1);

@@ -578,7 +578,7 @@ def run_config3(dev, hbm_gbs: float, reps: int = 3):
         plan.profile_enable(0)
         plan.set_option(lib_consts.OPT_OVERLAP, ov)
         half = 8.0 * (n // 2 + 1) / n
-        bpv = {"col_z_inv_filter": 2 * half, "col_y_inv": 2 * half, "row_c2r_ionize": half + 8.25}
+        bpv = {"col_z_inv_filter": 2 * half, "col_y_inv": 2 * half, "row_c2r_ionize": half + 8.0}
         passes = {}
         for k, b in bpv.items():
             ms, cnt = prof[k]
