@@ -16,7 +16,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libes_engine.so"
-SIZES = (32, 48, 64, 96, 128, 160, 256, 512)
+SIZES = (16, 32, 48, 64, 96, 128, 160, 256, 512, 1024)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}"]
 

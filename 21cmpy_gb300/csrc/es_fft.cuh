@@ -123,6 +123,7 @@ template <int N, int RS = 0> struct Plan;
     static constexpr int radix[] = {__VA_ARGS__};                          \
     static constexpr int stages = sizeof(radix) / sizeof(int);             \
   };
+ES_PLAN(8, 0, 8)
 ES_PLAN(16, 0, 16)
 ES_PLAN(24, 0, 8, 3)
 ES_PLAN(32, 0, 8, 4)
@@ -134,6 +135,8 @@ ES_PLAN(128, 0, 16, 8)
 ES_PLAN(160, 0, 8, 4, 5)
 ES_PLAN(256, 0, 16, 16)
 ES_PLAN(512, 0, 8, 8, 8)
+ES_PLAN(1024, 0, 16, 8, 8)
+ES_PLAN(8, 1, 4, 2)
 ES_PLAN(16, 1, 4, 4)
 ES_PLAN(24, 1, 8, 3)
 ES_PLAN(32, 1, 4, 8)
@@ -145,6 +148,7 @@ ES_PLAN(128, 1, 8, 4, 4)
 ES_PLAN(160, 1, 8, 4, 5)
 ES_PLAN(256, 1, 8, 8, 4)
 ES_PLAN(512, 1, 8, 8, 8)
+ES_PLAN(1024, 1, 8, 8, 4, 4)
 #undef ES_PLAN
 
 template <int N, int S, int RS = 0> struct StageNs {      // product of the radices before stage S

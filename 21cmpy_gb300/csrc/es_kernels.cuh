@@ -323,6 +323,7 @@ __device__ __forceinline__ void pk_finish(float* bins, const OpArgs& a) {
 
 // ------------------------------------------------------------------ column passes (y or z)
 template <int N> struct ColCfg;
+template <> struct ColCfg<16>  { static constexpr int TI = 8,  T = 64; };
 template <> struct ColCfg<32>  { static constexpr int TI = 16, T = 128; };
 template <> struct ColCfg<48>  { static constexpr int TI = 8,  T = 128; };
 template <> struct ColCfg<64>  { static constexpr int TI = 16, T = 128; };
@@ -331,6 +332,7 @@ template <> struct ColCfg<128> { static constexpr int TI = 16, T = 256; };
 template <> struct ColCfg<160> { static constexpr int TI = 16, T = 256; };
 template <> struct ColCfg<256> { static constexpr int TI = 16, T = 256; };
 template <> struct ColCfg<512> { static constexpr int TI = 8,  T = 256; };
+template <> struct ColCfg<1024> { static constexpr int TI = 4, T = 256; };
 
 template <int N, int MODE> struct ColSmem {
   static constexpr int TI = ColCfg<N>::TI, T = ColCfg<N>::T;
@@ -469,6 +471,7 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_pass(OpArgs a) {
 
 // ------------------------------------------------------------------ row passes (x)
 template <int N> struct RowCfg;
+template <> struct RowCfg<16>  { static constexpr int RL = 16, T = 64; };
 template <> struct RowCfg<32>  { static constexpr int RL = 16, T = 128; };
 template <> struct RowCfg<48>  { static constexpr int RL = 8,  T = 128; };
 template <> struct RowCfg<64>  { static constexpr int RL = 8,  T = 128; };
@@ -477,6 +480,7 @@ template <> struct RowCfg<128> { static constexpr int RL = 8,  T = 256; };
 template <> struct RowCfg<160> { static constexpr int RL = 8,  T = 256; };
 template <> struct RowCfg<256> { static constexpr int RL = 8,  T = 256; };
 template <> struct RowCfg<512> { static constexpr int RL = 4,  T = 256; };
+template <> struct RowCfg<1024> { static constexpr int RL = 2, T = 256; };
 
 template <int N> struct RowSmem {
   static constexpr int bytes = (N + 2 * RowCfg<N>::RL * (N / 2)) * 8;

@@ -36,7 +36,7 @@ struct OpGeometry {
 
 }  // namespace es
 
-#define ES_FOR_EACH_SIZE(X) X(32) X(48) X(64) X(96) X(128) X(160) X(256) X(512)
+#define ES_FOR_EACH_SIZE(X) X(16) X(32) X(48) X(64) X(96) X(128) X(160) X(256) X(512) X(1024)
 
 #define ES_HIDDEN __attribute__((visibility("hidden")))
 #define ES_DECLARE_SIZE(N)                                                                      \

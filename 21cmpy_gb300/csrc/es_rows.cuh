@@ -9,6 +9,7 @@
 namespace es {
 
 template <int N> struct Row2Cfg;
+template <> struct Row2Cfg<16>  { static constexpr int RL = 16, T = 128; };
 template <> struct Row2Cfg<32>  { static constexpr int RL = 16, T = 128; };
 template <> struct Row2Cfg<48>  { static constexpr int RL = 16, T = 128; };
 template <> struct Row2Cfg<64>  { static constexpr int RL = 16, T = 256; };
@@ -17,6 +18,7 @@ template <> struct Row2Cfg<128> { static constexpr int RL = 16, T = 256; };
 template <> struct Row2Cfg<160> { static constexpr int RL = 16, T = 256; };
 template <> struct Row2Cfg<256> { static constexpr int RL = 16, T = 256; };
 template <> struct Row2Cfg<512> { static constexpr int RL = 8,  T = 256; };
+template <> struct Row2Cfg<1024> { static constexpr int RL = 4, T = 256; };
 
 // Row-pass tile shapes: variant 0 = (RL rows, T threads) above, 1 = RL/2 rows with T/2 threads,
 // 2 = RL rows with T/2 threads, 3 = RL rows with 2T threads.

@@ -40,7 +40,7 @@ def test_host_only_calls(lib):
     buf = (C.c_int * 16)()
     n = lib.es_supported_sizes(buf, 16)
     sizes = [buf[i] for i in range(n)]
-    assert sizes == [32, 48, 64, 96, 128, 160, 256, 512]
+    assert sizes == [16, 32, 48, 64, 96, 128, 160, 256, 512, 1024]
     lib.es_plan_workspace_bytes.restype = C.c_size_t
     lib.es_plan_workspace_bytes.argtypes = [C.c_int, C.c_int]
     assert lib.es_plan_workspace_bytes(100, 10) == 0          # unsupported size

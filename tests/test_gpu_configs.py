@@ -6,7 +6,10 @@
   delta_T and P(k), the oracle on all host cores (scipy.fft workers);
 * sphere painting at 128^3 (find_bubbles.cu:73-140; radius R / cell in cells, periodic);
 * the uneven 64-box batch (HII_DIM ~ U{64, 96, 128, 160}): the plan-graph batch and the persistent
-  batched launch against per-box plans for every box, and the first 160^3 box against the oracle.
+  batched launch against per-box plans for every box, and the first 160^3 box against the oracle;
+* HII_DIM = 1024 through an exact property: a periodic 256^3 box tiled 4 x 4 x 4 (BOX_LEN x 4, the
+  same cells) has only the small box's modes, each with a bit-identical filter weight, so its
+  ionisation is the tiled 256^3 result, and so the tiled oracle's outside the exemption band.
 
 Bars: parity_util (flags except within 1e-5 of the threshold, mean x_HI and P(k) to 1e-4).
 delta_T and P(k) are checked on the engine's own x_HI (the oracle computes them from the same
@@ -134,3 +137,36 @@ def test_uneven_64_box_batch(eng):
     d, st = boxes[i160]
     ref = O.conv_bubbles(d.cpu().numpy(), st, tol=FLAG_TOL, backend="scipy", workers=WORKERS)
     compare_ionized(1.0 - per_box[i160][0].cpu().numpy().astype(np.float64), ref, "batch 160^3")
+
+
+@pytest.mark.skipif(os.environ.get("ES_SKIP_FULL") == "1", reason="full-size parity disabled")
+def test_1024_box_is_the_tiled_256_box(eng):
+    # DELTA_K = float32(2 pi / float32(L)) is exactly 4x smaller at L x 4, and |k|^2 of a tiled-box
+    # mode is 16x the small box's, so every filter argument dk sqrt(k2) R is the same float; only
+    # the transforms' rounding differs (different lengths)
+    n, L, z = 256, 300.0, 8.0
+    d = grf.density_box(n, L, seed=17, z=z)
+    st_s = sch.ionize_setup(n, L, z, zeta=30.0, t_vir_min=1e4, R_max=15.0, cosmo=cos.BASELINE_COSMO)
+    st_b = sch.ionize_setup(4 * n, 4 * L, z, zeta=30.0, t_vir_min=1e4, R_max=15.0, cosmo=cos.BASELINE_COSMO)
+    assert np.array_equal(st_s.radii(), st_b.radii()) and np.array_equal(st_s.denoms(), st_b.denoms())
+    assert float(np.float32(2 * np.pi / np.float32(L))) == 4 * float(np.float32(2 * np.pi / np.float32(4 * L)))
+    ref = O.conv_bubbles(d, st_s, tol=FLAG_TOL, backend="scipy", workers=WORKERS)
+    with eng.ExcursionSetPlan(n, L) as p:
+        small, nf_s = p.run(torch.from_numpy(d).cuda(), st_s, output="ionized")
+        small = small.cpu().numpy()
+    compare_ionized(small.astype(np.float64), ref, "256^3")
+    big_in = torch.from_numpy(d).cuda().repeat(4, 4, 4).contiguous()
+    with eng.ExcursionSetPlan(4 * n, 4 * L) as p:
+        big, nf_b = p.run(big_in, st_b, output="ionized")
+        p.check()
+    del big_in
+    tiled_ref = {"ionized": np.tile(ref["ionized"], (4, 4, 4)), "exempt": np.tile(ref["exempt"], (4, 4, 4)),
+                 "flags": np.tile(ref["flags"], (4, 4, 4))}
+    big_h = big.cpu().numpy()
+    del big
+    torch.cuda.empty_cache()
+    compare_ionized(big_h.astype(np.float64), tiled_ref, "1024^3 tiled")
+    # and cell by cell against the 256^3 engine result, outside the same band
+    diff = np.abs(big_h - np.tile(small, (4, 4, 4)))
+    assert ((diff > PARTIAL_ATOL) & ~tiled_ref["exempt"]).sum() == 0
+    assert abs(nf_b.item() - nf_s.item()) <= 1e-5

@@ -42,7 +42,7 @@ def _setup(n, L, z, **kw):
 _compare_ionized = compare_ionized
 
 
-@pytest.mark.parametrize("n", [32, 48, 64, 96, 128, 160])
+@pytest.mark.parametrize("n", [16, 32, 48, 64, 96, 128, 160])
 def test_fft_matches_numpy(eng, n):
     rng = np.random.default_rng(n)
     x = rng.standard_normal((n, n, n)).astype(np.float32)
@@ -56,7 +56,7 @@ def test_fft_matches_numpy(eng, n):
         assert err2 < 2e-6, f"inverse rel err {err2}"
 
 
-@pytest.mark.parametrize("n", [256, 512])
+@pytest.mark.parametrize("n", [256, 512, 1024])
 def test_fft_roundtrip_full_size(eng, n):
     # size-independent property at the benchmark sizes: c2r(r2c(x)) / n^3 == x, Parseval,
     # and agreement with torch.fft (cuFFT, used here only as a checker)
@@ -75,6 +75,7 @@ def test_fft_roundtrip_full_size(eng, n):
 
 CASES = [
     # (n, L, z, kwargs)
+    (16, 24.0, 8.0, dict(R_max=6.0)),
     (32, 48.0, 8.0, dict()),
     (64, 100.0, 8.0, dict()),                                   # the CPU-runnable 64^3 case
     (64, 100.0, 8.0, dict(filter_type=1)),
