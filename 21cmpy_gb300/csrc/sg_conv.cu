@@ -313,7 +313,11 @@ std::atomic<int> g_impl{SG_IMPL_AUTO};
 
 int sg_tc_conv_fwd(int cin, int cout, int mode, const void* in, const void* w, const float* bias, void* out,
                    const void* mask, cudaStream_t s, std::string* err);
+int sg_tc_conv_wgrad(int cin, int cout, const void* x, const void* dz, float* dw, float* db, float* ws,
+                     size_t ws_bytes, cudaStream_t s, std::string* err);
+size_t sg_tc_wgrad_workspace(int cout);
 int sg_tc_status(unsigned* status);
+int sg_tc_wgrad_diag(int* out4);
 
 extern "C" {
 
@@ -344,6 +348,11 @@ int sg_conv3d_wgrad(int n, int cin, int cout, const void* x, const void* dz, flo
   if (!shape_ok(n)) return sgfail(ES_E_ARG, "sg_conv3d_wgrad: n=%d must be a multiple of 16 in [16, %d]", n, sg::MAXN);
   if (!x || !dz || !dw || !db) return sgfail(ES_E_ARG, "sg_conv3d_wgrad: NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
+  if (n == 128 && g_impl.load() == SG_IMPL_AUTO) {
+    std::string err;
+    const int rc = sg_tc_conv_wgrad(cin, cout, x, dz, dw, db, ws, ws_bytes, s, &err);
+    return rc == ES_OK ? ES_OK : sgfail(rc, "sg_conv3d_wgrad: %s", err.c_str());
+  }
   if (cin == 16 && cout == 32) return launch_wgrad<16, 32>(n, x, dz, dw, db, ws, ws_bytes, s);
   if (cin == 32 && cout == 32) return launch_wgrad<32, 32>(n, x, dz, dw, db, ws, ws_bytes, s);
   if (cin == 32 && cout == 16) return launch_wgrad<32, 16>(n, x, dz, dw, db, ws, ws_bytes, s);
@@ -356,7 +365,10 @@ size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int chunks = (sms * 2 + 8) / 9;
   if (chunks > n * n) chunks = n * n;
-  return (size_t)9 * chunks * (27 * cout * cin + cout) * sizeof(float);
+  const size_t mma_sync = (size_t)9 * chunks * (27 * cout * cin + cout) * sizeof(float);
+  // at 128^3 either kernel family may run (sg_conv3d_set_impl): room for the larger
+  const size_t tc = n == 128 ? sg_tc_wgrad_workspace(cout) : 0;
+  return mma_sync > tc ? mma_sync : tc;
 }
 
 int sg_features(int n, const float* delta, float scale, const uint16_t* channels16, void* out, void* stream) {
@@ -388,7 +400,14 @@ int sg_check(void) {
   if (e != cudaSuccess) return sgfail(ES_E_CUDA, "sg_check: %s", cudaGetErrorString(e));
   unsigned st = 0;
   if (sg_tc_status(&st) != ES_OK) return sgfail(ES_E_CUDA, "sg_check: reading the device status failed");
-  if (st) return sgfail(ES_E_DEVICE, "sg_check: a tcgen05 convolution gave up a bounded wait (status %u)", st);
+  if (st) {
+    int d[4] = {0, 0, 0, 0};
+    sg_tc_wgrad_diag(d);
+    if (d[0])
+      return sgfail(ES_E_DEVICE, "sg_check: the tcgen05 weight gradient gave up a bounded wait (wait %d, item %d, "
+                    "CTA %d, progress %d)", d[0], d[1], d[2], d[3]);
+    return sgfail(ES_E_DEVICE, "sg_check: a tcgen05 convolution gave up a bounded wait (status %u)", st);
+  }
   return ES_OK;
 }
 

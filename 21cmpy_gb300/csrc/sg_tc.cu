@@ -447,6 +447,346 @@ __global__ void __launch_bounds__(THREADS, 1) conv_tc_kernel(const __nv_bfloat16
   }
 }
 
+// ------------------------------------------------------------------ weight gradient
+// dW[t][co][ci] = sum_v dZ[v][co] X[v + (dz, dy, dx)][ci] and db[co] = sum_v dZ[v][co] at 128^3.
+// With u = v + (0, 0, dx): dW = sum_u dZ[u - dx][co] X[u + (dz, dy, 0)][ci], so for one output row
+// (z, y) of dZ and one dy, one MMA per 16 voxels covers every (dz, ci) x (dx, co):
+//   A (M = 128, MN-major): the input rows z - 1, z, z + 1 at y + dy with 32 channel slots each, then
+//     a constant row of ones, whose products are the bias gradient;
+//   B (N = 3 COUT, MN-major): the dZ row (z, y) staged three times, shifted by dx = -1, 0, +1 (the
+//     circular wrap in x is applied while staging);
+//   D: one accumulator per dy (3 COUT columns of tensor memory), summed over all of the CTA's rows.
+// Staged rows hold, per 8-channel chunk, 128 voxel positions of 16 bytes: in MN-major terms the
+// core matrices (8 voxels x 8 channels) are 128 bytes apart along K and one chunk (2048 bytes)
+// apart along M / N, the same stride from a row's last chunk to the next row's first.  For
+// CIN = 16 the chunk slots 2 and 3 of a row are never written; they feed accumulator rows that are
+// not read.  Per-CTA partials [3][128][3 COUT] are summed in a fixed order by wgrad_tc_reduce.
+namespace wg {
+constexpr int CH = N * 16;                 // 2048 bytes per 8-channel chunk of a staged row
+constexpr int KCS = 4;                     // channel-chunk slots per staged input row
+constexpr int XROW = KCS * CH;             // 8192
+constexpr int XGROUP = 4 * XROW;           // rows z - 1, z, z + 1 and the ones row
+constexpr int XS = 4;                      // input-row groups: y - 1, y, y + 1 in use, y + 2 landing
+constexpr int DSL = 2;                     // dZ row slots
+constexpr int WINFLIGHT = 3;               // items (groups or dZ rows) a producer keeps in flight
+}  // namespace wg
+
+template <int CIN, int COUT> struct WLayout {
+  static constexpr int KC = CIN / 8, KCD = COUT / 8;
+  static constexpr int DCOPY = KCD * wg::CH;           // one shifted copy of a dZ row
+  static constexpr int DSLOT = 3 * DCOPY;
+  static constexpr int NCOLS = 3 * COUT;               // N of one MMA
+  static constexpr uint32_t TCOLS = 3 * NCOLS <= 256 ? 256u : 512u;
+  static constexpr int XRING = wg::XS * wg::XGROUP;
+  static constexpr int BAR_OFF = XRING + wg::DSL * DSLOT;
+  static constexpr int NBARS = 2 * wg::XS + 2 * wg::DSL + 1;    // xfull, xfree, dfull, dfree, done
+  static constexpr int BYTES = BAR_OFF + NBARS * 8 + 16 + 128;
+  static_assert(NCOLS % 16 == 0 && NCOLS <= 256, "N = 3 COUT must be a valid M = 128 MMA width");
+  static_assert(KC <= wg::KCS, "at most 32 input channels");
+  static_assert(BYTES <= 232448, "shared memory per CTA");
+};
+
+// Where a weight-gradient wait gave up: {tag, sequence number, CTA, progress of the MMA warp};
+// the first record wins.  Tags: 1 producer xfree, 2 producer dfree, 3 MMA xfull at a segment start,
+// 4 MMA xfull per row, 5 MMA dfull, 6 partials-out done.
+__device__ int g_wdiag[4];
+constexpr long kWSpin = 1L << 20;
+__device__ __forceinline__ bool wbar_wait(uint64_t* b, uint32_t parity, volatile int* abort, int tag, int seq, int prog) {
+  for (long i = 0; i < kWSpin; ++i) {
+    if (bar_try(b, parity)) return true;
+    if ((i & 255) == 255 && *abort) return false;
+  }
+  *abort = 1;
+  atomicOr(&g_err, ERR_TIMEOUT);
+  if (atomicCAS(&g_wdiag[0], 0, tag) == 0) {
+    g_wdiag[1] = seq;
+    g_wdiag[2] = (int)blockIdx.x;
+    g_wdiag[3] = prog;
+  }
+  return false;
+}
+
+// Shared-memory matrix descriptor, MN-major without swizzle: core matrices of 8 K-rows x 16 bytes
+// (8 elements along M or N), `lbo` between core matrices along K, `sbo` along M / N.
+__device__ __forceinline__ uint64_t mdesc_mn(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// kind::f16 instruction descriptor with both operands MN-major (transpose bits 15 and 16)
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int m, int n) { return idesc_bf16(m, n) | (1u << 15) | (1u << 16); }
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(THREADS, 1) wgrad_tc_kernel(const __nv_bfloat16* __restrict__ x,
+                                                              const __nv_bfloat16* __restrict__ dz,
+                                                              float* __restrict__ partials) {
+  using L = WLayout<CIN, COUT>;
+  constexpr int KC = L::KC, KCD = L::KCD;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  unsigned char* xring = sm;
+  unsigned char* dring = sm + L::XRING;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L::BAR_OFF);
+  uint64_t* xfull = bars;
+  uint64_t* xfree = bars + wg::XS;
+  uint64_t* dfull = bars + 2 * wg::XS;
+  uint64_t* dfree = bars + 2 * wg::XS + wg::DSL;
+  uint64_t* done = bars + 2 * wg::XS + 2 * wg::DSL;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + L::NBARS);
+  volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < wg::XS; ++i) {
+      bar_init(&xfull[i], PRODUCERS);
+      bar_init(&xfree[i], 1);
+    }
+    for (int i = 0; i < wg::DSL; ++i) {
+      bar_init(&dfull[i], PRODUCERS);
+      bar_init(&dfree[i], 1);
+    }
+    bar_init(done, 1);
+    *abort = 0;
+    fence_bar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, L::TCOLS);
+    tmem_relinquish();
+  }
+  // the ones row of every input-group slot (bf16 1.0 = 0x3F80), written once
+  {
+    const uint4 ones = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
+    for (int i = threadIdx.x; i < wg::XS * (wg::XROW / 16); i += THREADS) {
+      const int slot = i / (wg::XROW / 16), j = i % (wg::XROW / 16);
+      *reinterpret_cast<uint4*>(xring + slot * wg::XGROUP + 3 * wg::XROW + 16 * j) = ones;
+    }
+  }
+  fence_proxy_async();
+  tc_before();
+  __syncthreads();
+  tc_after();
+  const uint32_t tmem = *tmem_slot;
+  if (warp > MMA_WARP && warp <= MMA_WARP + 4) {
+    const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;
+    for (int c = 0; c < (int)L::TCOLS; c += 16) tmem_zero16(tmem + lanes + (uint32_t)c);
+    tmem_wait_st();
+  }
+  tc_before();
+  __syncthreads();
+  tc_after();
+  const Range rg = my_rows();
+
+  if (warp < MMA_WARP) {
+    // ------------------------------------------------------------------ copies
+    // Items in order, per z-plane segment [yb, ye) of the CTA's rows: X(yb - 1), X(yb), then per
+    // output row y: X(y + 1), dZ(y).  An item is published (proxy fence + arrive) once WINFLIGHT - 1
+    // newer ones are in flight, or at the end.
+    const int pt = threadIdx.x;
+    int nx = 0, nd = 0;                           // items issued of each kind
+    int kinds = 0;                                // bit i of the in-flight FIFO: 1 = dZ row
+    int pending = 0;                              // items issued but not yet published
+    int pub_x = 0, pub_d = 0;
+    auto publish_oldest = [&]() {
+      const bool isd = (kinds >> (pending - 1)) & 1;    // oldest at the highest bit
+      fence_proxy_async();
+      if (isd) bar_arrive(&dfull[pub_d++ % wg::DSL]);
+      else bar_arrive(&xfull[pub_x++ % wg::XS]);
+      --pending;
+      kinds &= (1 << pending) - 1;
+    };
+    auto after_issue = [&](bool isd) {
+      cp_async_commit();
+      kinds = (kinds << 1) | (isd ? 1 : 0);
+      ++pending;
+      if (pending >= wg::WINFLIGHT) {
+        cp_async_wait<wg::WINFLIGHT - 1>();       // the oldest pending item has landed
+        publish_oldest();
+      }
+    };
+    auto issue_x = [&](int z, int yw) -> bool {
+      const int slot = nx % wg::XS;
+      if (nx >= wg::XS && !wbar_wait(&xfree[slot], (uint32_t)((nx / wg::XS - 1) & 1), abort, 1, nx, nd)) return false;
+      unsigned char* gb = xring + slot * wg::XGROUP;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const __nv_bfloat16* src = x + (size_t)(((z + d + N - 1) % N) * N + yw) * N * CIN;
+        unsigned char* dst = gb + d * wg::XROW;
+        for (int c = pt; c < KC * N; c += PRODUCERS) {
+          const int kc = c % KC, v = c / KC;
+          cp_async16(dst + kc * wg::CH + v * 16, src + (size_t)v * CIN + kc * 8);
+        }
+      }
+      ++nx;
+      after_issue(false);
+      return true;
+    };
+    auto issue_d = [&](int r) -> bool {
+      const int slot = nd % wg::DSL;
+      if (nd >= wg::DSL && !wbar_wait(&dfree[slot], (uint32_t)((nd / wg::DSL - 1) & 1), abort, 2, nd, nx)) return false;
+      const __nv_bfloat16* src = dz + (size_t)r * N * COUT;
+      unsigned char* db = dring + slot * L::DSLOT;
+#pragma unroll
+      for (int sh = 0; sh < 3; ++sh) {               // copy sh holds dZ[(u - dx) mod N] at u, dx = sh - 1
+        unsigned char* dst = db + sh * L::DCOPY;
+        for (int c = pt; c < KCD * N; c += PRODUCERS) {
+          const int kc = c % KCD, u = c / KCD;
+          const int v = (u - (sh - 1) + N) % N;
+          cp_async16(dst + kc * wg::CH + u * 16, src + (size_t)v * COUT + kc * 8);
+        }
+      }
+      ++nd;
+      after_issue(true);
+      return true;
+    };
+    bool ok = true;
+    for (int r = rg.r0; r < rg.r1 && ok && !*abort;) {
+      const int z = r / N, yb = r % N;
+      const int ye = (z + 1) * N < rg.r1 ? N : rg.r1 - z * N;
+      ok = issue_x(z, (yb - 1 + N) % N) && issue_x(z, yb);
+      for (int y = yb; y < ye && ok && !*abort; ++y)
+        ok = issue_x(z, (y + 1) % N) && issue_d(z * N + y);
+      // The segment's last items are published now: the next segment opens with two input groups,
+      // and the second waits for the slot of a group that this segment's last row still reads.
+      cp_async_wait<0>();
+      if (ok && !*abort)
+        while (pending > 0) publish_oldest();
+      r = z * N + ye;
+    }
+    cp_async_wait<0>();
+    if (!*abort)
+      while (pending > 0) publish_oldest();
+  } else if (warp == MMA_WARP) {
+    // ---------------------------------------------------------------- MMA issue
+    const uint64_t a_base = mdesc_mn(saddr(xring), 128, wg::CH);
+    const uint64_t b_base = mdesc_mn(saddr(dring), 128, wg::CH);
+    constexpr uint32_t idesc = idesc_bf16_mn(128, L::NCOLS);
+    int gx = 0, gd = 0;
+    bool ok = true;
+    for (int r = rg.r0; r < rg.r1 && ok;) {
+      const int z = r / N, yb = r % N;
+      const int ye = (z + 1) * N < rg.r1 ? N : rg.r1 - z * N;
+      const int nrows = ye - yb;
+      ok = __all_sync(0xFFFFFFFFu, wbar_wait(&xfull[gx % wg::XS], (uint32_t)((gx / wg::XS) & 1), abort, 3, gx, gd)) &&
+           __all_sync(0xFFFFFFFFu, wbar_wait(&xfull[(gx + 1) % wg::XS], (uint32_t)(((gx + 1) / wg::XS) & 1), abort, 3, gx + 1, gd));
+      for (int i = 0; i < nrows && ok; ++i) {
+        const int gn = gx + i + 2;
+        ok = __all_sync(0xFFFFFFFFu, wbar_wait(&xfull[gn % wg::XS], (uint32_t)((gn / wg::XS) & 1), abort, 4, gn, gd)) &&
+             __all_sync(0xFFFFFFFFu, wbar_wait(&dfull[gd % wg::DSL], (uint32_t)((gd / wg::DSL) & 1), abort, 5, gd, gn));
+        if (!ok) break;
+        tc_after();
+        const uint64_t bd = b_base + (uint64_t)((gd % wg::DSL) * (L::DSLOT / 16));
+#pragma unroll
+        for (int dyi = 0; dyi < 3; ++dyi) {
+          const uint64_t ad = a_base + (uint64_t)(((gx + i + dyi) % wg::XS) * (wg::XGROUP / 16));
+          const uint32_t dcol = tmem + (uint32_t)(dyi * L::NCOLS);
+#pragma unroll
+          for (int ks = 0; ks < N / 16; ++ks) mma_acc(dcol, ad + (uint64_t)(ks * 16), bd + (uint64_t)(ks * 16), idesc);
+        }
+        mma_commit(&dfree[gd % wg::DSL]);           // this dZ row is not read again
+        mma_commit(&xfree[(gx + i) % wg::XS]);      // nor is input group y - 1
+        ++gd;
+      }
+      if (!ok) break;
+      mma_commit(&xfree[(gx + nrows) % wg::XS]);    // groups ye - 1 and ye end with the segment
+      mma_commit(&xfree[(gx + nrows + 1) % wg::XS]);
+      gx += nrows + 2;
+      r = z * N + ye;
+    }
+    __syncwarp();
+    mma_commit(done);                               // every MMA of this CTA, also after an abort
+    // the accumulators are freed only once every MMA issued has completed (bounded)
+    for (long i = 0; i < kWSpin && !bar_try(done, 0); ++i) {
+    }
+  } else {
+    // ------------------------------------------------------------------ partials out
+    const int q = warp & 3;
+    const uint32_t lanes = (uint32_t)(32 * q) << 16;
+    const bool ok = wbar_wait(done, 0, abort, 6, 0, 0);
+    if (__all_sync(0xFFFFFFFFu, ok)) {
+      tc_after();
+      const int m = 32 * q + lane;
+      float* dst = partials + (size_t)blockIdx.x * 3 * 128 * L::NCOLS;
+#pragma unroll
+      for (int dyi = 0; dyi < 3; ++dyi) {
+#pragma unroll
+        for (int c0 = 0; c0 < L::NCOLS; c0 += COUT) {
+          float v[COUT];
+          const uint32_t ta = tmem + lanes + (uint32_t)(dyi * L::NCOLS + c0);
+          if (COUT == 32) tmem_ld32(ta, v); else tmem_ld16(ta, v);
+          float* row = dst + ((size_t)dyi * 128 + m) * L::NCOLS + c0;
+#pragma unroll
+          for (int c = 0; c < COUT; c += 4) *reinterpret_cast<float4*>(row + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
+        }
+      }
+    }
+  }
+
+  tc_before();
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();
+    tc_after();
+    tmem_dealloc(tmem, L::TCOLS);
+  }
+}
+
+// dW[27][COUT][CIN] and db[COUT] from the per-CTA partials [cta][dy][(dz, ci) | ones][(dx, co)],
+// summed over CTAs in a fixed order.
+template <int CIN, int COUT>
+__global__ void wgrad_tc_reduce(const float* __restrict__ partials, int ctas, float* __restrict__ dw,
+                                float* __restrict__ db) {
+  constexpr int NCOLS = 3 * COUT, PER = 3 * 128 * NCOLS, NW = 27 * COUT * CIN;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NW + COUT; i += gridDim.x * blockDim.x) {
+    int dyi, m, n;
+    if (i < NW) {
+      const int t = i / (COUT * CIN), co = (i / CIN) % COUT, ci = i % CIN;
+      dyi = (t / 3) % 3;
+      m = (t / 9) * 32 + ci;
+      n = (t % 3) * COUT + co;
+    } else {
+      dyi = 1;
+      m = 96;                                      // the ones row
+      n = COUT + (i - NW);                         // the unshifted dZ copy
+    }
+    float s = 0.f;
+    for (int c = 0; c < ctas; ++c) s += partials[(size_t)c * PER + ((size_t)dyi * 128 + m) * NCOLS + n];
+    if (i < NW) dw[i] = s; else db[i - NW] = s;
+  }
+}
+
+template <int CIN, int COUT>
+int launch_wgrad(const void* x, const void* dz, float* dw, float* db, float* ws, size_t ws_bytes, cudaStream_t s,
+                 std::string* err) {
+  using L = WLayout<CIN, COUT>;
+  auto kern = wgrad_tc_kernel<CIN, COUT>;
+  static unsigned configured = 0u;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (!(configured & (1u << (dev & 31)))) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES) != cudaSuccess) {
+      *err = "tcgen05 wgrad: shared memory opt-in failed";
+      return ES_E_CUDA;
+    }
+    configured |= 1u << (dev & 31);
+  }
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t need = (size_t)sms * 3 * 128 * L::NCOLS * sizeof(float);
+  if (!ws || ws_bytes < need) {
+    *err = "tcgen05 wgrad: workspace needs " + std::to_string(need) + " bytes";
+    return ES_E_ARG;
+  }
+  kern<<<sms, THREADS, L::BYTES, s>>>((const __nv_bfloat16*)x, (const __nv_bfloat16*)dz, ws);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    wgrad_tc_reduce<CIN, COUT><<<64, 256, 0, s>>>(ws, sms, dw, db);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    *err = std::string("tcgen05 wgrad launch: ") + cudaGetErrorString(e);
+    return ES_E_CUDA;
+  }
+  return ES_OK;
+}
+
 // ------------------------------------------------------------------ host side
 template <int CIN, int COUT, int MODE>
 int launch(const void* in, const void* w, const float* bias, void* out, const void* mask, cudaStream_t s,
@@ -504,5 +844,37 @@ __attribute__((visibility("hidden"))) int sg_tc_status(unsigned* status) {
   unsigned zero = 0;
   cudaError_t e = cudaMemcpyFromSymbol(status, sgtc::g_err, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(sgtc::g_err, &zero, sizeof(unsigned));
+  return e == cudaSuccess ? ES_OK : ES_E_CUDA;
+}
+
+// Weight gradient at 128^3 on the tensor cores; ES_E_UNSUPPORTED for a combination not compiled.
+__attribute__((visibility("hidden"))) int sg_tc_conv_wgrad(int cin, int cout, const void* x, const void* dz, float* dw,
+                                                           float* db, float* ws, size_t ws_bytes, cudaStream_t s,
+                                                           std::string* err) {
+  using namespace sgtc;
+  if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(dz) | reinterpret_cast<uintptr_t>(ws)) & 15u) {
+    *err = "tcgen05 wgrad: tensors must be 16-byte aligned";
+    return ES_E_ARG;
+  }
+  if (cin == 16 && cout == 32) return launch_wgrad<16, 32>(x, dz, dw, db, ws, ws_bytes, s, err);
+  if (cin == 32 && cout == 32) return launch_wgrad<32, 32>(x, dz, dw, db, ws, ws_bytes, s, err);
+  if (cin == 32 && cout == 16) return launch_wgrad<32, 16>(x, dz, dw, db, ws, ws_bytes, s, err);
+  *err = "tcgen05 wgrad: combination not compiled";
+  return ES_E_UNSUPPORTED;
+}
+
+// Workspace of the tensor-core weight gradient (per-CTA partials).
+__attribute__((visibility("hidden"))) size_t sg_tc_wgrad_workspace(int cout) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return (size_t)sms * 3 * 128 * 3 * cout * sizeof(float);
+}
+
+// The weight gradient's wait record (see g_wdiag); reading clears it.
+__attribute__((visibility("hidden"))) int sg_tc_wgrad_diag(int* out4) {
+  int zero[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaMemcpyFromSymbol(out4, sgtc::g_wdiag, sizeof(zero));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(sgtc::g_wdiag, zero, sizeof(zero));
   return e == cudaSuccess ? ES_OK : ES_E_CUDA;
 }

@@ -142,6 +142,42 @@ def test_tcgen05_conv_matches_oracle_and_mma_sync(sg, cin, cout, mode):
         assert torch.isfinite(out_tc.float()).all()
 
 
+@pytest.mark.parametrize("cin,cout", [(16, 32), (32, 32), (32, 16)])
+def test_tcgen05_weight_gradient_matches_oracle_and_mma_sync(sg, cin, cout):
+    # 128^3: the tcgen05/TMEM weight gradient (MN-major operands, the ones row for the bias) against
+    # the mma.sync kernel on every tap, and against float64 sums on three taps and the bias
+    n = 128
+    lib = sg._lib.load()
+    g = torch.Generator().manual_seed(300 + cin + cout)
+    xb = _bf(torch.randn((n, n, n, cin), generator=g))
+    dzb = _bf(torch.randn((n, n, n, cout), generator=g))
+    net = sg.SurrogateNet()
+    res = []
+    for impl in (0, 1):
+        dw = torch.empty((27, cout, cin), device="cuda")
+        db = torch.empty(cout, device="cuda")
+        assert lib.sg_conv3d_set_impl(impl) == 0
+        try:
+            net._wgrad(n, cin, cout, xb.cuda(), dzb.cuda(), dw, db)
+            net._wgrad(n, cin, cout, xb.cuda(), dzb.cuda(), dw, db)     # twice: accumulators restart
+        finally:
+            lib.sg_conv3d_set_impl(0)
+        res.append((dw.cpu().double(), db.cpu().double()))
+    assert lib.sg_check() == 0
+    (dw_tc, db_tc), (dw_ms, db_ms) = res
+    assert _rel(dw_tc, dw_ms) < 1e-4 and _rel(db_tc, db_ms) < 1e-4     # fp32 sums, other orders
+    x64 = xb.double().numpy().reshape(-1, cin)
+    dz64 = dzb.double().numpy().reshape(-1, cout)
+    assert np.allclose(db_tc.numpy(), dz64.sum(0), rtol=1e-4, atol=1e-2)
+    xs = xb.double().numpy()
+    for t in (13, 0, 26):                               # (0,0,0), (-1,-1,-1), (+1,+1,+1)
+        dz_, dy_, dx_ = t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1
+        shifted = np.roll(xs, shift=(-dz_, -dy_, -dx_), axis=(0, 1, 2)).reshape(-1, cin)
+        ref = dz64.T @ shifted                           # [cout, cin]
+        err = np.abs(dw_tc[t].numpy() - ref).max() / np.abs(ref).max()
+        assert err < 1e-4, (t, err)
+
+
 def test_tcgen05_network_step_matches_mma_sync(sg):
     # one forward + backward of the full network at 128^3 on both kernel families
     n = 128
