@@ -728,13 +728,32 @@ def run_surrogate(dev, reps: int = 20):
 
     sg_ms = timed(lambda: net.forward(S.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)))
     eng_ms = timed(lambda: gen.plan.run(s.delta, st))
+    # one training step (forward keeping activations, backward with the weight gradients, Adam)
+    opt = S.Adam(net.parameters(), lr=3e-4)
+
+    def train_step():
+        f = S.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
+        pred, acts = net.forward(f, keep=True)
+        dws, dbs = net.backward(acts, pred, s.xH)
+        opt.step(dws + dbs, scale=1.0 / s.delta.numel())
+
+    step_ms = timed(train_step)
+    # the 32 -> 32 weight gradient alone (tensor cores at 128^3)
+    n = gen.n
+    xw = torch.randn((n, n, n, 32), device=dev).to(torch.bfloat16)
+    dzw = torch.randn((n, n, n, 32), device=dev).to(torch.bfloat16)
+    dw = torch.empty((27, 32, 32), device=dev)
+    db = torch.empty(32, device=dev)
+    wg_ms = timed(lambda: net._wgrad(n, 32, 32, xw, dzw, dw, db))
     net.check()
     flop = 2 * gen.n ** 3 * sum(27 * ci * co for ci, co in S.LAYERS)
+    wg_flop = 2 * n ** 3 * 27 * 32 * 32
     gen.plan.close()
     return {"workload": "one 128^3 box, BOX_LEN=200 Mpc, z=8, zeta=30, R_mfp=15 Mpc, Tvir=1e4 K",
             "boxes_per_s": 1e3 / sg_ms, "ms_per_box": sg_ms, "tflops": flop / sg_ms / 1e9,
             "engine_boxes_per_s": 1e3 / eng_ms, "engine_ms_per_box": eng_ms,
             "ratio_surrogate_over_engine": eng_ms / sg_ms,
+            "train_step_ms": step_ms, "wgrad_32x32_ms": wg_ms, "wgrad_32x32_tflops": wg_flop / wg_ms / 1e9,
             "note": "speed with random-init weights (it does not depend on them); accuracy of the trained "
                     "network against the plain engine is measured by Programs.train_surrogate"}
 
