@@ -34,6 +34,8 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--decay", type=float, default=0.8, help="step-size factor per epoch")
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--smooth", default=",".join(f"{r:g}" for r in S.SMOOTH_CELLS),
+                    help="radii (cells) of the smoothed input channels, comma-separated; empty for none")
     ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
     ap.add_argument("--conv-only", action="store_true",
@@ -53,7 +55,8 @@ def main(argv=None):
     t_data = time.time() - t0
     log(f"generated {len(train)} + {len(held)} pairs in {t_data:.1f} s")
 
-    net = S.SurrogateNet(seed=args.seed)
+    smoothing = tuple(float(v) for v in args.smooth.split(",") if v.strip())
+    net = S.SurrogateNet(seed=args.seed, smoothing=smoothing)
     untrained = S.evaluate(net, held, gen.plan)
     order_rng = np.random.default_rng(args.seed + 2)
     t0 = time.time()
@@ -70,7 +73,7 @@ def main(argv=None):
 
     # inference speed next to the plain engine (inputs resident on the device)
     s = held[0]
-    f = S.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
+    f = net.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
     st = S.schedule.ionize_setup(gen.n, gen.box_len, s.z, zeta=s.zeta, t_vir_min=s.t_vir, R_max=s.R_max,
                                  cosmo=gen.cosmo, table=gen.table)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -90,6 +93,7 @@ def main(argv=None):
         return min(times)
 
     sg_ms = best_ms(lambda: net.forward(f))
+    sg_in_ms = best_ms(lambda: net.forward(net.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)))
     eng_ms = best_ms(lambda: gen.plan.run(s.delta, st))
     from ..autotune import cached as tuned_config
     flop = 2 * gen.n ** 3 * sum(27 * ci * co for ci, co in S.LAYERS)
@@ -101,7 +105,9 @@ def main(argv=None):
         "epochs": args.epochs, "data_seconds": t_data, "train_seconds": t_train,
         "final_bce": float(np.mean(losses[-len(train):])) if losses else None,
         "trained": trained, "untrained": untrained, "constant_mean_abs_dxHI": const_err,
+        "smoothing_cells": list(smoothing),
         "surrogate_ms_per_box": sg_ms, "surrogate_boxes_per_s": 1e3 / sg_ms,
+        "surrogate_with_features_ms_per_box": sg_in_ms,
         "surrogate_tflops": flop / sg_ms / 1e9,
         "engine_ms_per_box": eng_ms, "engine_boxes_per_s": 1e3 / eng_ms, "engine_radii": st.n_radii,
         "engine_config": tuned_config(gen.plan.device, gen.n),

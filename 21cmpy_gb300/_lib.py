@@ -102,6 +102,8 @@ _PROTOS = {
     "sg_conv3d_set_impl": (C.c_int, [C.c_int]),
     "sg_conv3d_get_impl": (C.c_int, []),
     "sg_features": (C.c_int, [C.c_int, C.c_void_p, C.c_float, C.POINTER(C.c_uint16), C.c_void_p, C.c_void_p]),
+    "sg_features_ms": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.POINTER(C.c_uint16),
+                                 C.c_void_p, C.c_void_p]),
     "sg_check": (C.c_int, []),
     "sg_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "pf_plan_create": (C.c_int, [C.c_int, C.c_int, C.c_float, C.POINTER(C.c_void_p)]),

@@ -308,6 +308,28 @@ __global__ void features_kernel(long voxels, const float* __restrict__ delta, fl
     out[2 * v + 1] = make_uint4(c.w[4], c.w[5], c.w[6], c.w[7]);
   }
 }
+// Network input with smoothed copies of the density: channel 0 = bf16(delta * scale), channels
+// 1..4 the constant parameter bit patterns, channels 5 .. 4 + nsm = bf16(smoothed[j] * scale), the
+// rest the constant patterns (zero).  smoothed: nsm boxes of n^3 floats, one after another.
+__global__ void features_ms_kernel(long voxels, const float* __restrict__ delta, const float* __restrict__ smoothed,
+                                   int nsm, float scale, Feat16 c, uint4* __restrict__ out) {
+  for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < voxels; v += (long)gridDim.x * blockDim.x) {
+    uint32_t w[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) w[i] = c.w[i];
+    w[0] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(__ldg(delta + v) * scale)) | (w[0] & 0xFFFF0000u);
+#pragma unroll
+    for (int j = 0; j < 11; ++j) {
+      if (j < nsm) {
+        const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(__ldg(smoothed + (size_t)j * voxels + v) * scale));
+        const int ch = 5 + j, wi = ch / 2, sh = 16 * (ch & 1);
+        w[wi] = (w[wi] & ~(0xFFFFu << sh)) | (b << sh);
+      }
+    }
+    out[2 * v] = make_uint4(w[0], w[1], w[2], w[3]);
+    out[2 * v + 1] = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+}
 std::atomic<int> g_impl{SG_IMPL_AUTO};
 }  // namespace
 
@@ -385,6 +407,25 @@ int sg_features(int n, const float* delta, float scale, const uint16_t* channels
   features_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(voxels, delta, scale, c, (uint4*)out);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ES_OK : sgfail(ES_E_CUDA, "sg_features launch: %s", cudaGetErrorString(e));
+}
+
+int sg_features_ms(int n, const float* delta, const float* smoothed, int nsm, float scale, const uint16_t* channels16,
+                   void* out, void* stream) {
+  if (n < 1 || n > 2048 || !delta || !channels16 || !out || nsm < 0 || nsm > 11 || (nsm > 0 && !smoothed))
+    return sgfail(ES_E_ARG, "sg_features_ms: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(out) & 15u) != 0) return sgfail(ES_E_ARG, "sg_features_ms: out must be 16-byte aligned");
+  Feat16 c;
+  for (int i = 0; i < 8; ++i) c.w[i] = (uint32_t)channels16[2 * i] | ((uint32_t)channels16[2 * i + 1] << 16);
+  const long voxels = (long)n * n * n;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long blocks = (voxels + 255) / 256;
+  if (blocks > (long)sms * 16) blocks = (long)sms * 16;
+  features_ms_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(voxels, delta, smoothed, nsm, scale, c,
+                                                                         (uint4*)out);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ES_OK : sgfail(ES_E_CUDA, "sg_features_ms launch: %s", cudaGetErrorString(e));
 }
 
 int sg_conv3d_set_impl(int impl) {

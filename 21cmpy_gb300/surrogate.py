@@ -6,8 +6,12 @@ project's BF16 tensor-core kernels (``sg_conv3d_fwd`` / ``sg_conv3d_wgrad``, FP3
 Training pairs come from the plain engine; the plain engine is also the judge of the surrogate's
 error and its fallback (:class:`SurrogateSweep`).
 
-Channels-last BF16 activations [n][n][n][C].  Input features (16 channels, 5 used): normalised
-density delta / D(z), zeta / 80, R_mfp / 50, log10(T_vir) - 4, (z - 6) / 4.
+Channels-last BF16 activations [n][n][n][C].  Input features (16 channels, 5 + len(smoothing)
+used): normalised density delta / (4 D(z)), zeta / 80, R_mfp / 50, log10(T_vir) - 4, (z - 6) / 4,
+then the density smoothed with the real-space top hat of the excursion set (the engine's own
+transforms and window) at radii of 4, 8, 16 and 32 cells, scaled like channel 0.  Eight layers of
+3^3 kernels see +-8 cells; the excursion set's largest radius reaches 32 cells at 128^3 / 200 Mpc,
+and the smoothed channels hand the network that large-scale information directly.
 """
 from __future__ import annotations
 
@@ -21,6 +25,7 @@ import torch
 from . import _lib, cosmology, schedule
 
 LAYERS = [(16, 32)] + [(32, 32)] * 6 + [(32, 16)]      # (cin, cout); last: channel 0 is x_HI
+SMOOTH_CELLS = (4.0, 8.0, 16.0, 32.0)                 # radii (cells) of the smoothed input channels
 PARAM_RANGES = {"zeta": (10.0, 80.0), "R_max": (5.0, 50.0), "log10_tvir": (4.0, 5.3), "z": (6.0, 10.0)}
 
 
@@ -35,17 +40,21 @@ def _stream():
 class SurrogateNet:
     """Weights (FP32 masters) and the BF16 tensor-core forward / backward passes."""
 
-    def __init__(self, device=None, seed: int = 0):
+    def __init__(self, device=None, seed: int = 0, smoothing=SMOOTH_CELLS):
         self.lib = _lib.load()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.smoothing = tuple(float(r) for r in smoothing)
+        if len(self.smoothing) > 11:
+            raise ValueError("at most 11 smoothed input channels")
+        self.n_in = 5 + len(self.smoothing)
         g = torch.Generator(device="cpu").manual_seed(seed)
         self.w, self.b = [], []
         for li, (cin, cout) in enumerate(LAYERS):
-            used_in = 5 if li == 0 else cin
+            used_in = self.n_in if li == 0 else cin
             std = math.sqrt(2.0 / (27 * used_in))
             w = torch.randn((27, cout, cin), generator=g) * std
             if li == 0:
-                w[:, :, 5:] = 0.0
+                w[:, :, self.n_in:] = 0.0
             if li == len(LAYERS) - 1:
                 w[:, 1:, :] = 0.0
                 w *= 0.5
@@ -62,12 +71,21 @@ class SurrogateNet:
         _lib.check("sg_check", self.lib.sg_check(), self.lib)
 
     def load_state(self, state):
+        if tuple(state.get("smoothing", ())) != self.smoothing:
+            raise ValueError(f"weights were trained with smoothing {state.get('smoothing', ())}, "
+                             f"this network uses {self.smoothing}")
         for i, (w, b) in enumerate(zip(state["w"], state["b"])):
             self.w[i].copy_(w)
             self.b[i].copy_(b)
 
     def state(self):
-        return {"w": [w.detach().cpu() for w in self.w], "b": [b.detach().cpu() for b in self.b]}
+        return {"w": [w.detach().cpu() for w in self.w], "b": [b.detach().cpu() for b in self.b],
+                "smoothing": self.smoothing}
+
+    def features(self, delta: torch.Tensor, z: float, zeta: float, R_max: float, t_vir: float,
+                 cosmo=cosmology.BASELINE_COSMO) -> torch.Tensor:
+        """This network's input for a density box (with its smoothed channels)."""
+        return features(delta, z, zeta, R_max, t_vir, cosmo, smoothing=self.smoothing)
 
     # ------------------------------------------------------------------ kernels
     def _conv(self, n, cin, cout, mode, x, w, bias, out, mask=None):
@@ -125,15 +143,42 @@ class SurrogateNet:
                 self._conv(n, cout, cin, 2, dz, wflip, None, dprev, mask=acts[li])
                 dz = dprev
         # frozen entries: unused input channels of layer 0, unused outputs of the last layer
-        dws[0][:, :, 5:] = 0.0
+        dws[0][:, :, self.n_in:] = 0.0
         dws[-1][:, 1:, :] = 0.0
         dbs[-1][1:] = 0.0
         return dws, dbs
 
 
+_smooth_plans = {}
+
+
+def smoothed_fields(delta: torch.Tensor, radii_cells) -> torch.Tensor:
+    """The density smoothed with the real-space top hat W(kR) at each radius (in cells): one forward
+    transform, then per radius the window (``ic_shape``, the excursion set's filter) and an inverse
+    transform, all on the engine's kernels.  Returns float32 [len(radii), n, n, n]."""
+    from .engine import ExcursionSetPlan
+    n = delta.shape[0]
+    key = (n, str(delta.device))
+    if key not in _smooth_plans:
+        _smooth_plans[key] = ExcursionSetPlan(n, float(n), max_radii=1, device=delta.device)   # lengths in cells
+    plan = _smooth_plans[key]
+    lib = _lib.load()
+    out = torch.empty((len(radii_cells), n, n, n), dtype=torch.float32, device=delta.device)
+    with torch.cuda.device(delta.device):
+        X = plan.fft_r2c(delta)
+        Y = torch.empty_like(X)
+        for j, R in enumerate(radii_cells):
+            rc = lib.ic_shape(n, C.c_float(float(n)), _p(X), -1, 0, C.c_float(float(R)), 0, _p(Y), _stream())
+            _lib.check("ic_shape", rc, lib)
+            out[j] = plan.fft_c2r(Y)
+        out *= 1.0 / float(n) ** 3
+    return out
+
+
 def features(delta: torch.Tensor, z: float, zeta: float, R_max: float, t_vir: float,
-             cosmo=cosmology.BASELINE_COSMO) -> torch.Tensor:
-    """bf16 [n, n, n, 16] network input for a density box at redshift z and a parameter point."""
+             cosmo=cosmology.BASELINE_COSMO, smoothing=SMOOTH_CELLS) -> torch.Tensor:
+    """bf16 [n, n, n, 16] network input for a density box at redshift z and a parameter point:
+    density, the four parameters, and the density smoothed at the radii `smoothing` (cells)."""
     n = delta.shape[0]
     if not (isinstance(delta, torch.Tensor) and delta.is_cuda and delta.dtype == torch.float32
             and delta.is_contiguous() and tuple(delta.shape) == (n, n, n)):
@@ -144,9 +189,15 @@ def features(delta: torch.Tensor, z: float, zeta: float, R_max: float, t_vir: fl
     scale = float(np.float32(1.0 / (4.0 * cosmology.growth_factor(z, cosmo))))
     f = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=delta.device)
     lib = _lib.load()
+    smoothing = tuple(smoothing)
     with torch.cuda.device(delta.device):
-        rc = lib.sg_features(n, _p(delta), C.c_float(scale), bits, _p(f), _stream())
-    _lib.check("sg_features", rc, lib)
+        if smoothing:
+            sm = smoothed_fields(delta, smoothing)
+            rc = lib.sg_features_ms(n, _p(delta), _p(sm), len(smoothing), C.c_float(scale), bits, _p(f), _stream())
+            _lib.check("sg_features_ms", rc, lib)
+        else:
+            rc = lib.sg_features(n, _p(delta), C.c_float(scale), bits, _p(f), _stream())
+            _lib.check("sg_features", rc, lib)
     return f
 
 
@@ -239,7 +290,7 @@ def train(net: SurrogateNet, samples, epochs: int = 1, lr: float = 3e-4, log=Non
     losses = []
     for ep in range(epochs):
         for s in samples:
-            f = features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
+            f = net.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
             pred, acts = net.forward(f, keep=True)
             dws, dbs = net.backward(acts, pred, s.xH)
             nvox = float(s.delta.numel())
@@ -257,7 +308,7 @@ def evaluate(net: SurrogateNet, samples, plan=None, k_range=(0.1, 1.0), num_bins
     """Surrogate vs plain engine: mean |dx_HI|, flag agreement at 0.5, P21(k) ratio on k_range."""
     errs, agree, ratios = [], [], []
     for s in samples:
-        f = features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
+        f = net.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
         pred, _ = net.forward(f)
         errs.append((pred - s.xH).abs().mean().item())
         agree.append(((pred >= 0.5) == (s.xH >= 0.5)).float().mean().item())
@@ -274,7 +325,8 @@ def evaluate(net: SurrogateNet, samples, plan=None, k_range=(0.1, 1.0), num_bins
     r = np.concatenate(ratios) if ratios else np.zeros(0)
     return {"mean_abs_dxHI": float(np.mean(errs)), "flag_agreement": float(np.mean(agree)),
             "p21_ratio_median": float(np.median(r)) if r.size else None,
-            "p21_ratio_max_dev": float(np.max(np.abs(r - 1))) if r.size else None}
+            "p21_ratio_max_dev": float(np.max(np.abs(r - 1))) if r.size else None,
+            "p21_within_10pct": float(np.mean(np.abs(r - 1) <= 0.1)) if r.size else None}
 
 
 class SurrogateSweep:
@@ -313,7 +365,7 @@ class SurrogateSweep:
         check = bool(self.check_every) and self.calls % self.check_every == 0
         if not check and not self.trusted:
             return self._engine(delta, params), "engine"
-        pred, _ = self.net.forward(features(delta, params["z"], params["zeta"], params["R_max"], params["t_vir"]))
+        pred, _ = self.net.forward(self.net.features(delta, params["z"], params["zeta"], params["R_max"], params["t_vir"]))
         if check:
             ref = self._engine(delta, params)
             err = (pred - ref).abs().mean().item()

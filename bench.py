@@ -726,13 +726,13 @@ def run_surrogate(dev, reps: int = 20):
         e1.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    sg_ms = timed(lambda: net.forward(S.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)))
+    sg_ms = timed(lambda: net.forward(net.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)))
     eng_ms = timed(lambda: gen.plan.run(s.delta, st))
     # one training step (forward keeping activations, backward with the weight gradients, Adam)
     opt = S.Adam(net.parameters(), lr=3e-4)
 
     def train_step():
-        f = S.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
+        f = net.features(s.delta, s.z, s.zeta, s.R_max, s.t_vir)
         pred, acts = net.forward(f, keep=True)
         dws, dbs = net.backward(acts, pred, s.xH)
         opt.step(dws + dbs, scale=1.0 / s.delta.numel())

@@ -226,6 +226,11 @@ size_t sg_conv3d_wgrad_workspace(int n, int cin, int cout);
  * nearest even) and channels 1..15 = channels16[1..15] (bf16 bit patterns; channels16[0] unused).
  * delta: float [n^3] on the device; out 16-byte aligned. */
 int sg_features(int n, const float* delta, float scale, const uint16_t* channels16, void* out, void* stream);
+/* The same with nsm (0..11) smoothed copies of the density in channels 5 .. 4 + nsm:
+ * bf16(smoothed[j][voxel] * scale); smoothed holds nsm boxes of n^3 floats one after another.  No
+ * counterpart in the reference (network input of the surrogate). */
+int sg_features_ms(int n, const float* delta, const float* smoothed, int nsm, float scale, const uint16_t* channels16,
+                   void* out, void* stream);
 /* Which kernels sg_conv3d_fwd runs (process-wide, no counterpart in the reference):
  * SG_IMPL_AUTO = tcgen05/TMEM kernels for n = 128 (one CTA per SM, TMA-fed, accumulators in tensor
  * memory) and mma.sync kernels for other n; SG_IMPL_MMA_SYNC = mma.sync kernels for every n. */

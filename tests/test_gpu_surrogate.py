@@ -259,13 +259,26 @@ def test_features_kernel_and_cached_weights(sg):
     n = 32
     delta = torch.randn((n,) * 3, device="cuda") * 2.0
     z, zeta, rmax, tvir = 8.0, 30.0, 15.0, 2e4
-    f = sg.features(delta, z, zeta, rmax, tvir)
+    f = sg.features(delta, z, zeta, rmax, tvir, smoothing=())
     scale = np.float32(1.0 / (4.0 * cosm.growth_factor(z, cosm.BASELINE_COSMO)))
     ref0 = (delta * torch.tensor(float(scale), device="cuda")).to(torch.bfloat16)
     assert torch.equal(f[..., 0], ref0)
     const = torch.tensor([zeta / 80.0, rmax / 50.0, np.log10(tvir) - 4.0, (z - 6.0) / 4.0]).to(torch.bfloat16)
     assert torch.equal(f[..., 1:5], const.cuda().expand(n, n, n, 4))
     assert not f[..., 5:].any()
+    # with smoothed channels: channels 5..8 = bf16(delta smoothed with the top hat at 4, 8, 16, 32
+    # cells, times the same scale), the first five unchanged, the rest zero
+    fs = sg.features(delta, z, zeta, rmax, tvir)
+    assert torch.equal(fs[..., :5], f[..., :5]) and not fs[..., 9:].any()
+    d64 = delta.double().cpu().numpy()
+    X = np.fft.rfftn(d64)
+    k = np.sqrt(np.fft.fftfreq(n)[:, None, None] ** 2 + np.fft.fftfreq(n)[None, :, None] ** 2
+                + np.fft.rfftfreq(n)[None, None, :] ** 2) * 2 * np.pi       # per cell
+    from oracle import es_oracle as O
+    for j, R in enumerate(sg.SMOOTH_CELLS):
+        ref = np.fft.irfftn(X * O.rtophat(k * R), s=(n, n, n), axes=(0, 1, 2)) * float(scale)
+        got = fs[..., 5 + j].float().cpu().numpy()
+        assert np.abs(got - ref).max() <= 8e-3 * np.abs(ref).max() + 1e-6, (R, np.abs(got - ref).max())
     net = sg.SurrogateNet(seed=0)
     w0 = net.bf16_weights()
     assert net.bf16_weights() is w0
