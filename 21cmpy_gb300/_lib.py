@@ -63,7 +63,9 @@ class es_ionize_params(C.Structure):
 
 class es_batch_box(C.Structure):
     _fields_ = [("n", C.c_int), ("box_len", C.c_double), ("delta", C.c_void_p), ("out", C.c_void_p),
-                ("nf", C.c_void_p), ("params", es_ionize_params)]
+                ("nf", C.c_void_p), ("params", es_ionize_params), ("t_factor", C.c_float), ("dT", C.c_void_p),
+                ("ave", C.c_void_p), ("k2_thresholds", C.POINTER(C.c_int)), ("nbins", C.c_int),
+                ("dimensional", C.c_int), ("pk", C.c_void_p)]
 
 
 _PROTOS = {
@@ -91,6 +93,10 @@ _PROTOS = {
     "es_batch_check": (C.c_int, [C.c_void_p, C.c_void_p]),
     "es_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint),
                                 C.POINTER(C.c_int)]),
+    "es_batch_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "es_batch_get_schedule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint)]),
+    "es_batch_queue": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int]),
     "es_batch_destroy": (C.c_int, [C.c_void_p]),
     "es_batch_debug_stall": (C.c_int, [C.c_void_p, C.c_int, C.c_long]),
     "es_batch_last_error": (C.c_int, [C.c_char_p, C.c_int]),

@@ -9,6 +9,10 @@ best of those, the overlapped-radius schedules (``ES_OPT_OVERLAP`` with per-SM C
 ``ES_OPT_ROW_CTAS`` / ``ES_OPT_COL_CTAS``), then the runner-up tile shapes with the best schedule.  Results are cached per GPU model, box size and library version in a JSON file
 (``$ES_AUTOTUNE_CACHE`` or ``~/.cache/21cmpy_gb300/autotune.json``), so later plans of the same
 size start tuned.
+
+``tune_batch`` is the persistent batched launch's stage: it times the work-queue schedules
+(``es_batch_set_schedule``: boxes in flight x tiles per ticket) on the batch itself and keeps the
+fastest.
 """
 from __future__ import annotations
 
@@ -148,3 +152,30 @@ def ensure_tuned(plan, allow_tuning: bool = True):
     r = tune(plan)
     r["source"] = "tuned"
     return r
+
+
+# (lanes, tiles per ticket) of the persistent batched launch; lanes 0 = every box its own lane
+BATCH_SCHEDULES = [(0, 1), (4, 1), (8, 1), (16, 1), (8, 2), (16, 2), (8, 4), (16, 4), (32, 2)]
+
+
+def tune_batch(b, schedules=BATCH_SCHEDULES, repeats: int = 3) -> dict:
+    """Time every schedule on the batch ``b`` (a ``BatchedExcursionSet``), replaying its graph,
+    and leave the fastest set; returns {schedule: ms per batch}."""
+    dev = b.device
+    stream = torch.cuda.current_stream(dev)
+    times = {}
+    for lanes, chunk in schedules:
+        b.set_schedule(lanes, chunk)
+        b.run()
+        b.run()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(repeats):
+            b.run()
+        e1.record(stream)
+        e1.synchronize()
+        b.check()
+        times[(lanes, chunk)] = e0.elapsed_time(e1) / repeats
+    best = min(times, key=times.get)
+    b.set_schedule(*best)
+    return times

@@ -3,8 +3,9 @@ launch, replayed from a captured CUDA graph (no counterpart in the reference, wh
 per ``conv_bubbles`` call).
 
 Each box is a (device density, :class:`~.schedule.IonizeSetup`) pair; outputs are x_HI boxes and
-the mean x_HI of every box.  The persistent kernel walks a work queue of (box, pass, tile) items
-interleaved across boxes, so small boxes keep the whole GPU busy.
+the mean x_HI of every box.  The persistent kernel walks a work queue of (box, pass, tile) items:
+boxes are dealt to lanes balanced by N^3 * N_R and the lanes advance side by side, so small boxes
+keep the whole GPU busy while only a few boxes' workspaces are live at a time.
 """
 from __future__ import annotations
 
@@ -14,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .schedule import IonizeSetup
+from .schedule import IonizeSetup, pk_k2_thresholds
 
 
 def _params(st: IonizeSetup, output: int):
@@ -31,9 +32,16 @@ def _params(st: IonizeSetup, output: int):
 
 
 class BatchedExcursionSet:
-    """x_HI of many boxes in one persistent launch (``es_batch_*``)."""
+    """x_HI of many boxes in one persistent launch (``es_batch_*``).
 
-    def __init__(self, boxes, output: str = "xH", use_graph: bool = True, device=None):
+    ``t_factors`` (one brightness-temperature factor per box, see
+    ``cosmology.brightness_temperature_factor``) adds delta_T and its mean to every box's outputs,
+    and ``pk_edges`` (one array of bin edges in 1/Mpc per box, or one for all) its binned P(k)
+    (delta_T.py:73-98), all inside the same launch: ``self.dT``, ``self.ave`` and ``self.pk``
+    ((3, nbins) per box: ps_ave, k_ave, count)."""
+
+    def __init__(self, boxes, output: str = "xH", use_graph: bool = True, device=None, lanes: int = None,
+                 chunk: int = None, t_factors=None, pk_edges=None, dimensional: bool = False):
         if not torch.cuda.is_available():
             raise _lib.EngineUnavailable("the batched engine needs a CUDA device")
         self.lib = _lib.load()
@@ -46,8 +54,6 @@ class BatchedExcursionSet:
             n = st.n
             if tuple(d.shape) != (n, n, n) or not d.is_contiguous():
                 raise ValueError(f"density of a {n}^3 box must be a contiguous ({n}, {n}, {n}) tensor")
-            if st.update != 0:
-                raise ValueError("the batched engine supports centre-pixel updates only")
             self.inputs.append(d)
             self.setups.append(st)
         cnt = len(self.setups)
@@ -55,6 +61,21 @@ class BatchedExcursionSet:
             raise ValueError("empty batch")
         self.out = [torch.empty_like(d) for d in self.inputs]
         self.nf = torch.zeros(cnt, dtype=torch.float32, device=self.device)
+        self.dT = self.ave = self.pk = None
+        if pk_edges is not None and t_factors is None:
+            raise ValueError("P(k) is of delta_T: give t_factors too")
+        if t_factors is not None:
+            if len(t_factors) != cnt:
+                raise ValueError("one brightness-temperature factor per box")
+            self.dT = [torch.empty_like(d) for d in self.inputs]
+            self.ave = torch.zeros(cnt, dtype=torch.float32, device=self.device)
+        thr = [None] * cnt
+        if pk_edges is not None:
+            edges = [pk_edges] * cnt if np.ndim(pk_edges[0]) == 0 else list(pk_edges)
+            if len(edges) != cnt:
+                raise ValueError("one array of P(k) bin edges per box (or one for all)")
+            thr = [pk_k2_thresholds(st.n, st.box_len, np.asarray(e)) for st, e in zip(self.setups, edges)]
+            self.pk = [torch.zeros((3, len(t)), dtype=torch.float32, device=self.device) for t in thr]
         arr = (_lib.es_batch_box * cnt)()
         keep = []
         for i, (d, st) in enumerate(zip(self.inputs, self.setups)):
@@ -66,11 +87,35 @@ class BatchedExcursionSet:
             arr[i].out = C.c_void_p(self.out[i].data_ptr())
             arr[i].nf = C.c_void_p(self.nf.data_ptr() + 4 * i)
             arr[i].params = prm
+            if self.dT is not None:
+                arr[i].t_factor = float(t_factors[i])
+                arr[i].dT = C.c_void_p(self.dT[i].data_ptr())
+                arr[i].ave = C.c_void_p(self.ave.data_ptr() + 4 * i)
+            if thr[i] is not None:
+                cthr = (C.c_int * len(thr[i]))(*[int(v) for v in thr[i]])
+                keep.append(cthr)
+                arr[i].k2_thresholds = cthr
+                arr[i].nbins = len(thr[i])
+                arr[i].dimensional = int(dimensional)
+                arr[i].pk = C.c_void_p(self.pk[i].data_ptr())
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             rc = self.lib.es_batch_create(arr, cnt, C.byref(h))
         _lib.check("es_batch_create", rc, self.lib)
         self._h = h
+        if lanes is not None or chunk is not None:
+            self.set_schedule(0 if lanes is None else lanes, 1 if chunk is None else chunk)
+
+    def set_schedule(self, lanes: int, chunk: int):
+        """``lanes`` boxes in flight (0: every box its own lane), ``chunk`` tiles per ticket."""
+        _lib.check("es_batch_set_schedule", self.lib.es_batch_set_schedule(self.handle, int(lanes), int(chunk)),
+                   self.lib)
+
+    def schedule(self) -> dict:
+        lanes, chunk, tickets = C.c_int(), C.c_int(), C.c_uint()
+        _lib.check("es_batch_get_schedule", self.lib.es_batch_get_schedule(
+            self.handle, C.byref(lanes), C.byref(chunk), C.byref(tickets)), self.lib)
+        return {"lanes": lanes.value, "chunk": chunk.value, "tickets": tickets.value}
 
     @property
     def handle(self):
@@ -93,7 +138,7 @@ class BatchedExcursionSet:
         g, p, sm = C.c_int(), C.c_int(), C.c_int()
         t = C.c_uint()
         _lib.check("es_batch_info", self.lib.es_batch_info(self.handle, C.byref(g), C.byref(p), C.byref(t), C.byref(sm)), self.lib)
-        return {"grid": g.value, "passes": p.value, "tiles": t.value, "smem": sm.value}
+        return {"grid": g.value, "passes": p.value, "tiles": t.value, "smem": sm.value, **self.schedule()}
 
     def voxel_radius_updates(self) -> int:
         return sum(st.n ** 3 * st.n_radii for st in self.setups)
@@ -218,6 +263,33 @@ class PlanGraphBatch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+OPS = ("row_r2c", "y_fwd", "z_fwd", "z_inv", "y_inv", "row_c2r", "final", "wtab", "paint", "pk_r2c", "z_fwd_pk")
+
+
+def queue_plan(ns, n_radii, lanes: int = 0, chunk: int = 1, update=None, pk=None):
+    """The persistent launch's work queue for boxes of HII_DIM ``ns`` with ``n_radii`` radii (update
+    modes ``update`` and P(k) flags ``pk``, default all 0) under a schedule, built on the host by
+    ``es_batch_queue`` (no device needed): a list of {box, op, radius, tiles, first, tickets, dep,
+    dep2} in queue order."""
+    lib = _lib.load()
+    cnt = len(ns)
+    upd = [0] * cnt if update is None else [int(u) for u in update]
+    pks = [0] * cnt if pk is None else [int(u) for u in pk]
+    n_arr = (C.c_int * cnt)(*[int(v) for v in ns])
+    r_arr = (C.c_int * cnt)(*[int(v) for v in n_radii])
+    u_arr = (C.c_int * cnt)(*upd)
+    k_arr = (C.c_int * cnt)(*pks)
+    cap = sum(5 + 3 * int(r) + (int(r) - 1 if u else 0) + 3 * k for r, u, k in zip(n_radii, upd, pks))
+    out = (C.c_int * (8 * cap))()
+    rc = lib.es_batch_queue(n_arr, r_arr, u_arr, k_arr, cnt, int(lanes), int(chunk), out, cap)
+    _lib.check("es_batch_queue", min(rc, 0), lib)
+    keys = ("box", "op", "radius", "tiles", "first", "tickets", "dep", "dep2")
+    q = [dict(zip(keys, out[8 * k:8 * k + 8])) for k in range(rc)]
+    for d in q:
+        d["op"] = OPS[d["op"]]
+    return q
 
 
 def boxes_from_specs(specs, device=None, cosmo=None, table=None):

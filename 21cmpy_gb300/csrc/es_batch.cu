@@ -1,14 +1,20 @@
 // Batched excursion-set engine: many boxes of uneven HII_DIM (and their own zeta, R_mfp, T_vir,
 // z) run in ONE persistent launch.  The host lists every box's passes (forward transform, three
-// passes per radius, final step) level by level, interleaving the boxes; CTAs take tiles from a
-// global ticket counter in that order.  A pass of a box starts once the box's previous pass has
-// counted all its tiles done, so tiles only ever wait on tiles with smaller tickets, all held by
+// passes per radius, final step) and merges them into one work queue: the boxes are dealt to
+// `lanes` lanes (balanced by N^3 * N_R), a lane runs its boxes one after the other, and the lanes
+// advance side by side in proportion to work done, so only `lanes` boxes' workspaces are live at a
+// time (they stay in L2 at these sizes).  CTAs take tickets of `chunk` tiles from a global counter
+// in queue order.  A pass waits until its dependencies (at most two earlier passes of its box)
+// have counted all their tickets done.  The filtered spectrum alternates between two buffers by
+// radius parity, so the z inverse of radius r + 1 depends only on the row pass of radius r - 1 and
+// overlaps radius r's y and row passes.  Dependencies always point to earlier tickets, all held by
 // resident CTAs: the queue cannot deadlock.  Every wait is bounded; a timeout raises the batch's
 // error word and an abort flag that makes every CTA leave.
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -24,9 +30,15 @@ constexpr int FINAL_PAIRS = 2048;    // voxel pairs per final-step tile
 constexpr long kSpinLimit = 1L << 24;          // polls of 100 ns before a wait is declared hung
 constexpr unsigned ES_DEV_ERR_BATCH_TIMEOUT = 2u;
 
-enum BOp { B_ROW_R2C = 0, B_COL_Y_FWD = 1, B_COL_Z_FWD = 2, B_COL_Z_INV = 3, B_COL_Y_INV = 4, B_ROW_C2R = 5, B_FINAL = 6 };
+enum BOp { B_ROW_R2C = 0, B_COL_Y_FWD = 1, B_COL_Z_FWD = 2, B_COL_Z_INV = 3, B_COL_Y_INV = 4, B_ROW_C2R = 5, B_FINAL = 6,
+           B_WTAB = 7, B_PAINT = 8, B_PK_R2C = 9, B_COL_Z_FWD_PK = 10 };
+constexpr int WTAB_TILE = 2048;      // filter-table entries per tile
+constexpr int PAINT_TILES = 64;      // tiles of a painting pass (8 warps each, one centre per warp at a time)
+// P(k) binning's shared memory after a column tile's buffers: per-warp bins [8][3][PK_MAX_BINS],
+// per-warp scratch [8][32][4], the bin thresholds
+constexpr int PK_SMEM = (8 * 3 * PK_MAX_BINS + 8 * 32 * 4 + PK_MAX_BINS) * 4;
 
-struct RadB { float R, denom; int k2cut, pad; };
+struct RadB { float R, denom; int k2cut, r2max; };   // r2max: sphere painting's largest |d|^2 (-1: none)
 
 struct BoxDev {
   int n, n_radii, normalize, filter, ref_compat, output;
@@ -34,21 +46,36 @@ struct BoxDev {
   const float* delta;
   float* out;
   float* nf;
-  float2 *X, *Xnyq, *T, *Tnyq;
+  float2 *X, *Xnyq, *T[2], *Tnyq[2];  // filtered spectrum: one buffer per radius parity
+  float* wtab;           // [n_radii][k2n]: W(k^2) * growth / N^3 of every radius, k^2 = 0 .. 3 (N/2)^2
+  int k2n, update;       // table row length; 1: sphere painting
+  uint32_t* centers;     // sphere mode: centres found by the current row pass
+  unsigned* ccount;      // [n_radii]: centres found by the row pass of each radius
   float *dR0, *dR1;
   unsigned long long* flags;
   const float2* tw;
   const RadB* rad;
   float* stats;          // [n_radii][4]: sum, mean, norm
   float* partials;       // per-tile partial sums of the reducing passes
-  unsigned* arrive;      // [n_radii + 1] arrival counters
+  unsigned* arrive;      // [n_radii + 3] arrival counters: row passes, final step, delta_T mean, P(k)
+  // delta_T and P(k) (delta_T.py:73-98): tfac = 0 skips both, nbins = 0 skips P(k)
+  float tfac, pk_norm, volume;
+  int nbins, dimensional, pad1;
+  float* dT;
+  float* ave;
+  const int* thr;        // [nbins] k^2 thresholds
+  float* pk_out;         // [3 nbins]
+  float* pk_part;        // [z tiles][3 nbins] per-tile bins (counts as unsigned)
+  float* partials2;      // per-tile partial sums of delta_T
 };
 
-struct PassDesc { int box, op, radius, tiles, first, dep, need, pad; };   // need: done count awaited on dep
+// first: first ticket; dep/dep2: passes awaited (-1: none), need/need2: their ticket counts
+struct PassDesc { int box, op, radius, tiles, first, tickets, dep, need, dep2, need2, pad0, pad1; };
 
 struct BatchArgs {
   const BoxDev* boxes;
   const PassDesc* passes;
+  const int* first;    // first ticket of every pass (a compact copy for the search)
   int npasses;
   unsigned total;
   unsigned* ticket;
@@ -56,6 +83,7 @@ struct BatchArgs {
   unsigned* err;
   unsigned* abort;
   long spin_limit;
+  int chunk;           // tiles per ticket
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -64,18 +92,30 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-template <int N> struct BCol { static constexpr int TI = ColCfg<N>::TI; };
-template <int N> struct BRow { static constexpr int RL = N >= 256 ? 8 : 16; };
+// column tiles: TI columns x N rows; row tiles: RL rows of N/2 complex pairs
+template <int N> struct BCol { static constexpr int TI = 8; };
+template <int N> struct BRow { static constexpr int RL = N >= 128 ? 8 : 16; };
 
 template <int N> __host__ __device__ constexpr int col_tiles_z() { return N * ((N / 2) / BCol<N>::TI) + N / BCol<N>::TI; }
 template <int N> __host__ __device__ constexpr int col_tiles_y() { return N * ((N / 2) / BCol<N>::TI); }
 template <int N> __host__ __device__ constexpr int row_tiles() { return N * N / BRow<N>::RL; }
 template <int N> __host__ __device__ constexpr int final_tiles() { return (N * N * (N / 2) + FINAL_PAIRS - 1) / FINAL_PAIRS; }
+// column passes: twiddles, two tile buffers (one landing while the other is transformed) and the
+// transform's second buffer; row passes: twiddles, the transform's two
+// buffers, two raw-row buffers and the previous radius's delta_R tile
 template <int N> __host__ __device__ constexpr int smem_bytes() {
-  constexpr int col = (N + 2 * N * BCol<N>::TI) * 8;
-  constexpr int row = (N + 2 * (N / 2) * (BRow<N>::RL + 1)) * 8;
+  constexpr int TI = BCol<N>::TI, RL = BRow<N>::RL, M = N / 2;
+  constexpr int col = (N + 3 * N * TI) * 8;
+  constexpr int row = (N + 2 * M * (RL + 1) + 3 * RL * M) * 8;
   return col > row ? col : row;
 }
+
+__device__ __forceinline__ void cp16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+               ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(__cvta_generic_to_global(src)) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int K> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory"); }
 
 __device__ float block_sum_b(float v, float* sred) { return block_sum<BT>(v, sred); }
 
@@ -98,79 +138,210 @@ __device__ bool tile_reduce(float mine, float* partials, unsigned* arrive, int t
   return true;
 }
 
-// ---------------------------------------------------------------- column tiles (y or z)
-template <int N, int OP>
-__device__ __noinline__ void b_col(const BoxDev& b, int radius, int tile, float2* sm) {
-  constexpr int M = N / 2, TI = BCol<N>::TI, CPR = M / TI;
-  constexpr bool INV = OP == B_COL_Z_INV || OP == B_COL_Y_INV;
-  constexpr bool Z = OP == B_COL_Z_FWD || OP == B_COL_Z_INV;
-  float2* tw = sm;
-  float2* A = tw + N;
-  float2* B = A + N * TI;
-  for (int i = threadIdx.x; i < N; i += BT) tw[i] = __ldg(b.tw + i);
-  bool nyq = false;
-  int c, plane;
-  size_t off, es_g;
-  if (Z) {
-    if (tile < N * CPR) { plane = tile / CPR; c = tile % CPR; off = (size_t)plane * M + c * TI; es_g = (size_t)N * M; }
-    else { nyq = true; plane = 0; c = tile - N * CPR; off = (size_t)c * TI; es_g = N; }
-  } else {
-    plane = tile / CPR; c = tile % CPR; off = (size_t)plane * N * M + c * TI; es_g = M;
-  }
-  const float2* src = OP == B_COL_Z_INV ? (nyq ? b.Xnyq : b.X) : (nyq ? b.Tnyq : b.T);
-  if (OP == B_COL_Y_FWD || OP == B_COL_Z_FWD) src = nyq ? b.Xnyq : b.X;
-  float2* dst = OP == B_COL_Y_FWD || OP == B_COL_Z_FWD ? (nyq ? b.Xnyq : b.X) : (nyq ? b.Tnyq : b.T);
-  // z inverse: W depends on |k|^2 = kz^2 + (the column's ky^2 + kx^2), N/2 + 1 distinct values per
-  // column; they go into B (free until the transform) before the tile is loaded
-  float* wcol = reinterpret_cast<float*>(B);
-  if (OP == B_COL_Z_INV) {
-    const RadB rd = b.rad[radius];
-    const float sc = b.growth * b.inv_n3;
-    for (int q = threadIdx.x; q < TI * (M + 1); q += BT) {
-      const int col = q / (M + 1), kz = q % (M + 1);
-      const int ck2 = !nyq ? wrap2<N>(plane) + (c * TI + col) * (c * TI + col) : wrap2<N>(c * TI + col) + M * M;
-      wcol[q] = filter_weight(kz * kz + ck2, b.dk, rd.R, rd.k2cut, b.filter, b.ref_compat) * sc;
-    }
-    __syncthreads();
-  }
-  for (int e = threadIdx.x; e < N * TI; e += BT) {
+// ---------------------------------------------------------------- P(k) (delta_T.py:84-98)
+// Spherical binning of one z-forward tile of g's spectrum: k^3 |G|^2 / (2 pi^2 V), |k| and the mode
+// count (1, or 2 for kx > 0 of the half spectrum) into per-warp bins, warp-aggregated per bin;
+// arithmetic as the per-box plan's binning.
+template <int N, int TI>
+__device__ __forceinline__ void pk_bin_tile(const BoxDev& b, int plane, int c, bool nyq, const float2* Rr, float* bins,
+                                            float* scratch, const int* sthr) {
+  constexpr int M = N / 2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* wb = bins + warp * PK_MAX_BINS * 3;
+  float* ws = scratch + warp * 32 * 4;
+  const float inv = 1.0f / (2.0f * 9.8696044010893586f * b.volume);
+  for (int e = threadIdx.x; e < N * TI; e += BT) {       // whole warps iterate together
     const int row = e / TI, col = e % TI;
-    float2 v = __ldcg(src + off + row * es_g + col);
-    if (OP == B_COL_Z_INV) v = cscale(v, wcol[col * (M + 1) + (row > M ? N - row : row)]);
-    A[e] = v;
+    int k2;
+    float wgt;
+    if (!nyq) { const int kx = c * TI + col; k2 = wrap2<N>(row) + wrap2<N>(plane) + kx * kx; wgt = kx == 0 ? 1.f : 2.f; }
+    else { k2 = wrap2<N>(row) + wrap2<N>(c * TI + col) + M * M; wgt = 1.f; }
+    int lo = 0, hi = b.nbins;                            // first bin with k2 <= thr[bin]
+    while (lo < hi) { const int mid = (lo + hi) >> 1; if (k2 <= sthr[mid]) hi = mid; else lo = mid + 1; }
+    int bin = lo;
+    if (k2 == 0) bin = b.nbins;                          // the mean (k = 0) is excluded
+    const float2 gk = Rr[e];
+    const float km = b.dk * sqrtf((float)k2);
+    ws[lane * 4 + 0] = wgt * km * km * km * (gk.x * gk.x + gk.y * gk.y) * inv;
+    ws[lane * 4 + 1] = wgt * km;
+    reinterpret_cast<unsigned*>(ws)[lane * 4 + 2] = (unsigned)wgt;
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    __syncwarp();
+    if (bin < b.nbins && lane == __ffs(peers) - 1) {
+      float p = 0.f, k = 0.f;
+      unsigned n = 0u;
+      unsigned m = peers;
+      while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1;
+        p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += reinterpret_cast<const unsigned*>(ws)[l * 4 + 2];
+      }
+      wb[bin] += p; wb[PK_MAX_BINS + bin] += k; reinterpret_cast<unsigned*>(wb)[2 * PK_MAX_BINS + bin] += n;
+    }
+    __syncwarp();
   }
-  if (OP == B_COL_Y_INV && c == 0) {
-    __syncthreads();
-    for (int j = threadIdx.x; j < N; j += BT) {
-      const float2 y0 = A[j * TI];
-      const float2 ym = __ldcg(b.Tnyq + (size_t)plane * N + j);
-      A[j * TI] = make_float2(y0.x - ym.y, y0.y + ym.x);
+}
+
+// The tile's bins (warps summed in a fixed order) go to its slot of the per-tile partials; the
+// last tile of the pass to arrive sums the slots in tile order (lanes over tiles, a fixed
+// butterfly), so P(k) does not depend on which CTA ran which tile, and writes the bin means.
+template <int N>
+__device__ __forceinline__ void pk_tile_done(const BoxDev& b, int tile, float* bins, float* scratch) {
+  __shared__ unsigned s_last;
+  const int nb = b.nbins, nb3 = 3 * nb, tiles = col_tiles_z<N>();
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < nb3; idx += BT) {
+    const int q = idx / nb, bin = idx % nb;
+    if (q < 2) {
+      float acc = 0.f;
+      for (int w = 0; w < 8; ++w) acc += bins[w * PK_MAX_BINS * 3 + q * PK_MAX_BINS + bin];
+      b.pk_part[(size_t)tile * nb3 + idx] = acc;
+    } else {
+      unsigned acc = 0u;
+      for (int w = 0; w < 8; ++w) acc += reinterpret_cast<const unsigned*>(bins + w * PK_MAX_BINS * 3)[2 * PK_MAX_BINS + bin];
+      reinterpret_cast<unsigned*>(b.pk_part)[(size_t)tile * nb3 + idx] = acc;
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(b.arrive + b.n_radii + 2, 1u) == (unsigned)tiles - 1) ? 1u : 0u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* tot = scratch;                                  // [3 nb] <= 384 floats, inside the scratch
+  for (int idx = warp; idx < nb3; idx += BT / 32) {
+    if (idx < 2 * nb) {
+      float acc = 0.f;
+      for (int t = lane; t < tiles; t += 32) acc += __ldcg(b.pk_part + (size_t)t * nb3 + idx);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) tot[idx] = acc;
+    } else {
+      unsigned acc = 0u;
+      for (int t = lane; t < tiles; t += 32) acc += __ldcg(reinterpret_cast<const unsigned*>(b.pk_part) + (size_t)t * nb3 + idx);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) tot[idx] = __uint2float_rn(acc);
     }
   }
   __syncthreads();
-  float2* Rr = fft_lines<N, INV, TI, BT, true, TI, 1, N>(A, B, tw);
-  if (OP == B_COL_Y_FWD && c == 0) {
-    for (int e = threadIdx.x; e < N * TI; e += BT) {
-      const int row = e / TI, col = e % TI;
-      if (col == 0) {
-        const float2 v = Rr[row * TI];
-        const float2 w = Rr[((N - row) % N) * TI];
-        dst[off + row * es_g] = make_float2(0.5f * (v.x + w.x), 0.5f * (v.y - w.y));
-        b.Xnyq[(size_t)plane * N + row] = make_float2(0.5f * (v.y + w.y), -0.5f * (v.x - w.x));
-      } else {
-        dst[off + row * es_g + col] = Rr[e];
+  for (int bin = threadIdx.x; bin < nb; bin += BT) {
+    const float n = tot[2 * nb + bin];
+    b.pk_out[bin] = n > 0.f ? tot[bin] / n : 0.f;                 // ps_ave
+    b.pk_out[nb + bin] = n > 0.f ? tot[nb + bin] / n : 0.f;       // k_ave
+    b.pk_out[2 * nb + bin] = n;                                   // count
+  }
+}
+
+// The tiles [t0, t1) of one column pass, software-pipelined: tile t + 1's columns land in shared
+// memory (cp.async, 16 bytes per copy) while tile t is transformed.
+template <int N, int OP>
+__device__ __noinline__ void b_col_chunk(const BoxDev& b, int radius, int t0, int t1, float2* sm) {
+  constexpr int M = N / 2, TI = BCol<N>::TI, CPR = M / TI;
+  constexpr bool INV = OP == B_COL_Z_INV || OP == B_COL_Y_INV;
+  constexpr bool PK = OP == B_COL_Z_FWD_PK;
+  constexpr bool Z = OP == B_COL_Z_FWD || OP == B_COL_Z_INV || PK;
+  constexpr bool FWD = OP == B_COL_Y_FWD || OP == B_COL_Z_FWD || PK;
+  float2* tw = sm;
+  float2* const abuf0 = tw + N;
+  float2* const abuf1 = abuf0 + N * TI;
+  float2* B = abuf1 + N * TI;
+  float* bins = reinterpret_cast<float*>(B + N * TI);          // P(k): [8][3][PK_MAX_BINS]
+  float* scratch = bins + 8 * 3 * PK_MAX_BINS;                  // [8][32][4]
+  int* sthr = reinterpret_cast<int*>(scratch + 8 * 32 * 4);     // [PK_MAX_BINS]
+  if (PK)
+    for (int i = threadIdx.x; i < b.nbins; i += BT) sthr[i] = __ldg(b.thr + i);
+  for (int i = threadIdx.x; i < N; i += BT) tw[i] = __ldg(b.tw + i);
+  float2* const T = b.T[radius & 1];
+  float2* const Tnyq = b.Tnyq[radius & 1];
+  struct Geo { int plane, c; size_t off, es_g; bool nyq; };
+  auto geom = [&](int tile) {
+    Geo g;
+    g.nyq = false;
+    if (Z) {
+      if (tile < N * CPR) { g.plane = tile / CPR; g.c = tile % CPR; g.off = (size_t)g.plane * M + g.c * TI; g.es_g = (size_t)N * M; }
+      else { g.nyq = true; g.plane = 0; g.c = tile - N * CPR; g.off = (size_t)g.c * TI; g.es_g = N; }
+    } else {
+      g.plane = tile / CPR; g.c = tile % CPR; g.off = (size_t)g.plane * N * M + g.c * TI; g.es_g = M;
+    }
+    return g;
+  };
+  auto source = [&](const Geo& g) -> const float2* {
+    if (OP == B_COL_Z_INV || FWD) return g.nyq ? b.Xnyq : b.X;
+    return g.nyq ? Tnyq : T;
+  };
+  auto issue = [&](int tile, float2* buf) {
+    const Geo g = geom(tile);
+    const float2* src = source(g) + g.off;
+    for (int q = threadIdx.x; q < N * TI / 2; q += BT) {
+      const int row = q / (TI / 2), col = 2 * (q % (TI / 2));
+      cp16(buf + row * TI + col, src + row * g.es_g + col);
+    }
+    cp_commit();
+  };
+  issue(t0, abuf0);
+  for (int tile = t0; tile < t1; ++tile) {
+    float2* A = ((tile - t0) & 1) ? abuf1 : abuf0;
+    const bool more = tile + 1 < t1;
+    if (more) issue(tile + 1, ((tile - t0) & 1) ? abuf0 : abuf1);
+    const Geo g = geom(tile);
+    float2* dst = FWD ? (g.nyq ? b.Xnyq : b.X) : (g.nyq ? Tnyq : T);
+    if (PK)
+      for (int i = threadIdx.x; i < 8 * 3 * PK_MAX_BINS; i += BT) bins[i] = 0.f;
+    if (more) cp_wait<1>(); else cp_wait<0>();
+    __syncthreads();
+    if (OP == B_COL_Z_INV) {
+      // W depends on |k|^2 = kz^2 + (the column's ky^2 + kx^2) only: the radius's table row
+      const float* wt = b.wtab + (size_t)radius * b.k2n;
+      for (int e = threadIdx.x; e < N * TI; e += BT) {
+        const int row = e / TI, col = e % TI;
+        const int kz = row > M ? N - row : row;
+        const int ck2 = !g.nyq ? wrap2<N>(g.plane) + (g.c * TI + col) * (g.c * TI + col)
+                               : wrap2<N>(g.c * TI + col) + M * M;
+        A[e] = cscale(A[e], __ldg(wt + kz * kz + ck2));
+      }
+      __syncthreads();
+    }
+    if (OP == B_COL_Y_INV && g.c == 0) {
+      for (int j = threadIdx.x; j < N; j += BT) {
+        const float2 y0 = A[j * TI];
+        const float2 ym = __ldcg(Tnyq + (size_t)g.plane * N + j);
+        A[j * TI] = make_float2(y0.x - ym.y, y0.y + ym.x);
+      }
+      __syncthreads();
+    }
+    float2* Rr = fft_lines<N, INV, TI, BT, true, TI, 1, N>(A, B, tw);
+    if (PK) {
+      pk_bin_tile<N, TI>(b, g.plane, g.c, g.nyq, Rr, bins, scratch, sthr);
+      pk_tile_done<N>(b, tile, bins, scratch);
+    } else if (OP == B_COL_Y_FWD && g.c == 0) {
+      for (int e = threadIdx.x; e < N * TI; e += BT) {
+        const int row = e / TI, col = e % TI;
+        if (col == 0) {
+          const float2 v = Rr[row * TI];
+          const float2 w = Rr[((N - row) % N) * TI];
+          dst[g.off + row * g.es_g] = make_float2(0.5f * (v.x + w.x), 0.5f * (v.y - w.y));
+          b.Xnyq[(size_t)g.plane * N + row] = make_float2(0.5f * (v.y + w.y), -0.5f * (v.x - w.x));
+        } else {
+          dst[g.off + row * g.es_g + col] = Rr[e];
+        }
+      }
+    } else {
+      for (int q = threadIdx.x; q < N * TI / 2; q += BT) {        // 16-byte stores
+        const int row = q / (TI / 2), col = 2 * (q % (TI / 2));
+        const float2 v0 = Rr[row * TI + col], v1 = Rr[row * TI + col + 1];
+        *reinterpret_cast<float4*>(dst + g.off + row * g.es_g + col) = make_float4(v0.x, v0.y, v1.x, v1.y);
       }
     }
-  } else {
-    for (int e = threadIdx.x; e < N * TI; e += BT) {
-      const int row = e / TI, col = e % TI;
-      dst[off + row * es_g + col] = Rr[e];
-    }
+    __syncthreads();                     // A and B are reused by the next tile
   }
 }
 
 // ---------------------------------------------------------------- row tiles (x), transposed layout
-template <int N>
+// x R2C of the density, or (PK) of g = (delta_T / ave - 1) V / N^3 (times ave when dimensional),
+// the per-box plan's P(k) prologue (delta_T.py:80-82)
+template <int N, bool PK>
 __device__ __noinline__ void b_row_r2c(const BoxDev& b, int tile, float2* sm) {
   constexpr int M = N / 2, RL = BRow<N>::RL, ES = RL + 1;
   float2* tw = sm;
@@ -178,10 +349,19 @@ __device__ __noinline__ void b_row_r2c(const BoxDev& b, int tile, float2* sm) {
   float2* B = A + M * ES;
   for (int i = threadIdx.x; i < N; i += BT) tw[i] = __ldg(b.tw + i);
   const size_t pair0 = (size_t)tile * RL * M;
-  const float2* in = reinterpret_cast<const float2*>(b.delta) + pair0;
+  const float2* in = reinterpret_cast<const float2*>(PK ? b.dT : b.delta) + pair0;
+  float sc = 1.f, sh = 0.f;
+  if (PK) {
+    const float ave = __ldcg(b.ave);
+    sc = b.pk_norm / ave;
+    sh = -b.pk_norm;
+    if (b.dimensional) { sc *= ave; sh *= ave; }
+  }
   for (int e = threadIdx.x; e < RL * M; e += BT) {
     const int row = e / M, p = e % M;
-    A[p * ES + row] = __ldg(in + e);
+    float2 v = PK ? __ldcg(in + e) : __ldg(in + e);
+    if (PK) v = make_float2(fmaf(v.x, sc, sh), fmaf(v.y, sc, sh));
+    A[p * ES + row] = v;
   }
   __syncthreads();
   float2* Z = fft_lines<M, false, RL, BT, true, ES, 1, N>(A, B, tw);
@@ -206,39 +386,23 @@ __device__ __noinline__ void b_row_r2c(const BoxDev& b, int tile, float2* sm) {
   }
 }
 
+// The tiles [t0, t1) of one row pass (x C2R + ionisation epilogue), software-pipelined: tile
+// t + 1's rows and tile t's previous-radius delta_R land in shared memory (cp.async) while tile t
+// is split and transformed.  Arithmetic as b_row_c2r.
 template <int N>
-__device__ __noinline__ void b_row_c2r(const BoxDev& b, int radius, int tile, float2* sm, float* sred) {
+__device__ __noinline__ void b_row_c2r_chunk(const BoxDev& b, int radius, int t0, int t1, float2* sm, float* sred) {
   constexpr int M = N / 2, RL = BRow<N>::RL, ES = RL + 1;
   float2* tw = sm;
   float2* A = tw + N;
   float2* B = A + M * ES;
+  float2* const raw0 = B + M * ES;
+  float2* const raw1 = raw0 + RL * M;
+  float2* const P = raw1 + RL * M;
   for (int i = threadIdx.x; i < N; i += BT) tw[i] = __ldg(b.tw + i);
-  __syncthreads();                                        // the split below reads the twiddles
-  const size_t pair0 = (size_t)tile * RL * M;
-  const float2* src = b.T + pair0;
-  // item t of row l makes Z[t] and Z[M-t] (item 0: Z[0] from (X[0], X[N/2]) and Z[M/2])
-  for (int q = threadIdx.x; q < RL * (M / 2); q += BT) {
-    const int t = q % (M / 2), l = q / (M / 2);
-    const float2* x = src + (size_t)l * M;
-    if (t == 0) {
-      const float2 x0 = __ldcg(x), xh = __ldcg(x + M / 2);
-      A[l] = make_float2(x0.x + x0.y, x0.x - x0.y);
-      const float2 th = cmul(cconj(tw[M / 2]), make_float2(0.f, xh.y + xh.y));
-      A[(M / 2) * ES + l] = make_float2(xh.x + xh.x - th.y, th.x);
-    } else {
-      const int m2 = M - t;
-      const float2 xm = __ldcg(x + t), xc = __ldcg(x + m2), w = tw[t];
-      const float2 t1 = cmul(cconj(w), make_float2(xm.x - xc.x, xm.y + xc.y));
-      A[t * ES + l] = make_float2(xm.x + xc.x - t1.y, xm.y - xc.y + t1.x);
-      const float2 t2 = cmul(make_float2(-w.x, -w.y), make_float2(xc.x - xm.x, xc.y + xm.y));   // conj w^(M-t)
-      A[m2 * ES + l] = make_float2(xc.x + xm.x - t2.y, xc.y - xm.y + t2.x);
-    }
-  }
-  __syncthreads();
-  float2* Zr = fft_lines<M, true, RL, BT, true, ES, 1, N>(A, B, tw);
   const bool has_prev = radius > 0;
   float2* cur = reinterpret_cast<float2*>((radius & 1) ? b.dR1 : b.dR0);
   const float2* prv = reinterpret_cast<const float2*>((radius & 1) ? b.dR0 : b.dR1);
+  const float2* srcT = b.T[radius & 1];
   float thr = __int_as_float(0x7f800000);
   if (has_prev) {
     const float y = b.inv_zeta / __ldcg(b.stats + 4 * (radius - 1) + 2);
@@ -246,26 +410,98 @@ __device__ __noinline__ void b_row_c2r(const BoxDev& b, int radius, int tile, fl
   }
   const float inv_denom = 1.0f / b.rad[radius].denom, dc = b.dc;
   const int lane = threadIdx.x & 31;
-  float acc = 0.f;
-  for (int e = threadIdx.x; e < RL * M; e += BT) {       // whole warps: 64 consecutive voxels
-    const int row = e / M, p = e % M;
-    const float2 d = Zr[p * ES + row];
-    acc += erfc_sum_term((dc - d.x) * inv_denom) + erfc_sum_term((dc - d.y) * inv_denom);
-    if (has_prev) {
-      const float2 pp = __ldcg(prv + pair0 + e);
-      const unsigned bx = __ballot_sync(0xffffffffu, pp.x >= thr);
-      const unsigned by = __ballot_sync(0xffffffffu, pp.y >= thr);
-      if (lane == 0 && (bx | by)) atomicOr(b.flags + (pair0 + e) / 32, ((unsigned long long)by << 32) | bx);
+  auto issue_rows = [&](const float2* src, size_t pair0, float2* buf) {
+    for (int q = threadIdx.x; q < RL * M / 2; q += BT) cp16(buf + 2 * q, src + pair0 + 2 * q);
+    cp_commit();
+  };
+  issue_rows(srcT, (size_t)t0 * RL * M, raw0);
+  for (int tile = t0; tile < t1; ++tile) {
+    const size_t pair0 = (size_t)tile * RL * M;
+    const float2* raw = ((tile - t0) & 1) ? raw1 : raw0;
+    const bool more = tile + 1 < t1;
+    if (has_prev) issue_rows(prv, pair0, P); else cp_commit();
+    if (more) issue_rows(srcT, pair0 + RL * M, ((tile - t0) & 1) ? raw0 : raw1);
+    if (more) cp_wait<2>(); else cp_wait<1>();
+    __syncthreads();
+    // item t of row l makes Z[t] and Z[M-t] (item 0: Z[0] from (X[0], X[N/2]) and Z[M/2])
+    for (int q = threadIdx.x; q < RL * (M / 2); q += BT) {
+      const int t = q % (M / 2), l = q / (M / 2);
+      const float2* x = raw + l * M;
+      if (t == 0) {
+        const float2 x0 = x[0], xh = x[M / 2];
+        A[l] = make_float2(x0.x + x0.y, x0.x - x0.y);
+        const float2 th = cmul(cconj(tw[M / 2]), make_float2(0.f, xh.y + xh.y));
+        A[(M / 2) * ES + l] = make_float2(xh.x + xh.x - th.y, th.x);
+      } else {
+        const int m2 = M - t;
+        const float2 xm = x[t], xc = x[m2], w = tw[t];
+        const float2 t1v = cmul(cconj(w), make_float2(xm.x - xc.x, xm.y + xc.y));
+        A[t * ES + l] = make_float2(xm.x + xc.x - t1v.y, xm.y - xc.y + t1v.x);
+        const float2 t2v = cmul(make_float2(-w.x, -w.y), make_float2(xc.x - xm.x, xc.y + xm.y));   // conj w^(M-t)
+        A[m2 * ES + l] = make_float2(xc.x + xm.x - t2v.y, xc.y - xm.y + t2v.x);
+      }
     }
-    cur[pair0 + e] = d;
+    __syncthreads();
+    float2* Zr = fft_lines<M, true, RL, BT, true, ES, 1, N>(A, B, tw);
+    if (more) cp_wait<1>(); else cp_wait<0>();
+    __syncthreads();
+    float acc = 0.f;
+    for (int e = threadIdx.x; e < RL * M; e += BT) {     // whole warps: 64 consecutive voxels
+      const int row = e / M, p = e % M;
+      const float2 d = Zr[p * ES + row];
+      acc += erfc_sum_term((dc - d.x) * inv_denom) + erfc_sum_term((dc - d.y) * inv_denom);
+      if (has_prev) {
+        const float2 pp = P[e];
+        const bool px = pp.x >= thr, py = pp.y >= thr;
+        const unsigned bx = __ballot_sync(0xffffffffu, px);
+        const unsigned by = __ballot_sync(0xffffffffu, py);
+        if (!b.update) {
+          if (lane == 0 && (bx | by)) atomicOr(b.flags + (pair0 + e) / 32, ((unsigned long long)by << 32) | bx);
+        } else if (bx | by) {              // sphere mode: list the centres for the painting pass
+          unsigned first = 0;
+          if (lane == 0) first = atomicAdd(b.ccount + radius, __popc(bx) + __popc(by));
+          first = __shfl_sync(0xffffffffu, first, 0);
+          const unsigned lt = (1u << lane) - 1u;
+          const uint32_t v0 = (uint32_t)((pair0 + e) * 2);
+          unsigned pos = first + __popc(bx & lt) + __popc(by & lt);
+          if (px) b.centers[pos++] = v0;
+          if (py) b.centers[pos] = v0 + 1;
+        }
+      }
+      cur[pair0 + e] = d;
+    }
+    float total;
+    if (tile_reduce(acc, b.partials, b.arrive + radius, tile, row_tiles<N>(), sred, &total) && threadIdx.x == 0) {
+      const float mean = total * b.inv_n3;
+      b.stats[4 * radius + 0] = total;
+      b.stats[4 * radius + 1] = mean;
+      b.stats[4 * radius + 2] = b.normalize ? b.fc_mean / mean : 1.f;
+    }
+    __syncthreads();                     // A, B, the raw rows and P are reused by the next tile
   }
-  float total;
-  if (tile_reduce(acc, b.partials, b.arrive + radius, tile, row_tiles<N>(), sred, &total) && threadIdx.x == 0) {
-    const float mean = total * b.inv_n3;
-    b.stats[4 * radius + 0] = total;
-    b.stats[4 * radius + 1] = mean;
-    b.stats[4 * radius + 2] = b.normalize ? b.fc_mean / mean : 1.f;
+}
+
+// Filter table of every radius: W(k^2) * growth / N^3 for k^2 = 0 .. 3 (N/2)^2, the same product
+// the per-box plans form per column (filter_weight, find_bubbles.cu:14-41).
+__device__ __noinline__ void b_wtab(const BoxDev& b, int tile) {
+  const long total = (long)b.n_radii * b.k2n;
+  const float sc = b.growth * b.inv_n3;
+  for (long i = (long)tile * WTAB_TILE + threadIdx.x; i < (long)(tile + 1) * WTAB_TILE && i < total; i += BT) {
+    const int r = (int)(i / b.k2n), k2 = (int)(i % b.k2n);
+    const RadB rd = b.rad[r];
+    b.wtab[i] = filter_weight(k2, b.dk, rd.R, rd.k2cut, b.filter, b.ref_compat) * sc;
   }
+}
+
+// Sphere painting of the centres the row pass of `radius` found (they passed at radius - 1, so
+// the ball has radius - 1's size); periodic, or clipped to the box in the reference's mode.
+__device__ __noinline__ void b_paint(const BoxDev& b, int radius, int tile) {
+  const unsigned cnt = __ldcg(b.ccount + radius);
+  const int r2max = b.rad[radius - 1].r2max;
+  if (r2max < 0) return;
+  const int warp = threadIdx.x >> 5;
+  for (unsigned ci = tile * (BT / 32) + warp; ci < cnt; ci += PAINT_TILES * (BT / 32))
+    paint_ball(__ldcg(b.centers + ci), b.n, r2max, b.ref_compat ? 0 : 1, reinterpret_cast<uint32_t*>(b.flags));
 }
 
 template <int N>
@@ -275,7 +511,8 @@ __device__ __noinline__ void b_final(const BoxDev& b, int tile, float* sred) {
   const float norm = __ldcg(b.stats + 4 * last + 2), denom = b.rad[last].denom;
   const long pairs = (long)N * N * (N / 2);
   const long p0 = (long)tile * FINAL_PAIRS;
-  float acc = 0.f;
+  const bool dt = b.tfac != 0.f;
+  float acc = 0.f, acc_t = 0.f;
   for (long p = p0 + threadIdx.x; p < p0 + FINAL_PAIRS && p < pairs; p += BT) {
     const float2 d = __ldcg(dR + p);
     const unsigned long long w = __ldcg(b.flags + p / 32);
@@ -291,71 +528,119 @@ __device__ __noinline__ void b_final(const BoxDev& b, int tile, float* sred) {
     acc += (1.0f - ion[0]) + (1.0f - ion[1]);
     reinterpret_cast<float2*>(b.out)[p] =
         b.output == 0 ? make_float2(1.0f - ion[0], 1.0f - ion[1]) : make_float2(ion[0], ion[1]);
+    if (dt) {                                          // delta_T.py:75: c x_HI (1 + delta)
+      const float2 dd = __ldg(reinterpret_cast<const float2*>(b.delta) + p);
+      const float2 t = make_float2(b.tfac * (1.0f - ion[0]) * (1.0f + dd.x), b.tfac * (1.0f - ion[1]) * (1.0f + dd.y));
+      acc_t += t.x + t.y;
+      reinterpret_cast<float2*>(b.dT)[p] = t;
+    }
   }
   float total;
   if (tile_reduce(acc, b.partials, b.arrive + b.n_radii, tile, final_tiles<N>(), sred, &total) && threadIdx.x == 0)
     *b.nf = total * b.inv_n3;
+  if (dt) {
+    __syncthreads();
+    if (tile_reduce(acc_t, b.partials2, b.arrive + b.n_radii + 1, tile, final_tiles<N>(), sred, &total) &&
+        threadIdx.x == 0)
+      *b.ave = total * b.inv_n3;
+  }
 }
 
 template <int N>
 __device__ __forceinline__ void run_item(const BoxDev& b, const PassDesc& pd, int tile, float2* sm, float* sred) {
   switch (pd.op) {
-    case B_ROW_R2C: b_row_r2c<N>(b, tile, sm); break;
-    case B_COL_Y_FWD: b_col<N, B_COL_Y_FWD>(b, 0, tile, sm); break;
-    case B_COL_Z_FWD: b_col<N, B_COL_Z_FWD>(b, 0, tile, sm); break;
-    case B_COL_Z_INV: b_col<N, B_COL_Z_INV>(b, pd.radius, tile, sm); break;
-    case B_COL_Y_INV: b_col<N, B_COL_Y_INV>(b, pd.radius, tile, sm); break;
-    case B_ROW_C2R: b_row_c2r<N>(b, pd.radius, tile, sm, sred); break;
+    case B_ROW_R2C: b_row_r2c<N, false>(b, tile, sm); break;
+    case B_PK_R2C: b_row_r2c<N, true>(b, tile, sm); break;
     case B_FINAL: b_final<N>(b, tile, sred); break;
+    case B_WTAB: b_wtab(b, tile); break;
+    case B_PAINT: b_paint(b, pd.radius, tile); break;
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void run_chunk(const BoxDev& b, const PassDesc& pd, int t0, int t1, float2* sm, float* sred) {
+  switch (pd.op) {
+    case B_COL_Y_FWD: b_col_chunk<N, B_COL_Y_FWD>(b, 0, t0, t1, sm); return;
+    case B_COL_Z_FWD: b_col_chunk<N, B_COL_Z_FWD>(b, 0, t0, t1, sm); return;
+    case B_COL_Z_INV: b_col_chunk<N, B_COL_Z_INV>(b, pd.radius, t0, t1, sm); return;
+    case B_COL_Y_INV: b_col_chunk<N, B_COL_Y_INV>(b, pd.radius, t0, t1, sm); return;
+    case B_COL_Z_FWD_PK: b_col_chunk<N, B_COL_Z_FWD_PK>(b, 0, t0, t1, sm); return;
+    case B_ROW_C2R: b_row_c2r_chunk<N>(b, pd.radius, t0, t1, sm, sred); return;
+    default:
+      for (int tile = t0; tile < t1; ++tile) {
+        run_item<N>(b, pd, tile, sm, sred);
+        __syncthreads();                                 // shared memory is reused by the next tile
+      }
   }
 }
 
 #define ESB_SIZES(X) X(32) X(48) X(64) X(96) X(128) X(160) X(256)
 
-__global__ void __launch_bounds__(BT) batch_kernel(BatchArgs g) {
+__global__ void __launch_bounds__(BT, 4) batch_kernel(BatchArgs g) {
   extern __shared__ float4 smem4[];
   float2* sm = reinterpret_cast<float2*>(smem4);
   __shared__ float sred[BT / 32];
-  __shared__ unsigned s_t;
-  __shared__ int s_go;
+  __shared__ unsigned s_t, s_next;
+  __shared__ int s_pass, s_go;
+  const int lane = threadIdx.x & 31;
+  int cursor = 0;                                       // pass of this CTA's previous ticket
+  if (threadIdx.x == 0) s_t = atomicAdd(g.ticket, 1u);
+  __syncthreads();
   for (;;) {
-    if (threadIdx.x == 0) {
-      s_t = *(volatile unsigned*)g.abort ? g.total : atomicAdd(g.ticket, 1u);
-    }
-    __syncthreads();
     const unsigned t = s_t;
     if (t >= g.total) break;
-    int lo = 0, hi = g.npasses - 1;                       // pass holding ticket t
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if ((unsigned)g.passes[mid].first <= t) lo = mid; else hi = mid - 1;
-    }
-    const PassDesc pd = g.passes[lo];
-    if (threadIdx.x == 0) {
-      int go = 1;
-      if (pd.dep >= 0) {
-        const unsigned need = (unsigned)pd.need;
+    if (threadIdx.x < 32) {
+      // the next ticket is taken now, so its latency hides behind this one's work; tickets only
+      // grow, so the pass holding t is at or after the previous ticket's (32-ary search)
+      unsigned nxt = 0;
+      if (lane == 0) nxt = atomicAdd(g.ticket, 1u);
+      int lo = cursor, hi = g.npasses;
+      while (hi - lo > 1) {
+        const int step = (hi - lo + 31) / 32;
+        const int idx = lo + lane * step;
+        const bool le = idx < hi && (unsigned)__ldg(g.first + idx) <= t;
+        const unsigned m = __ballot_sync(0xffffffffu, le);   // bit 0 set: first[lo] <= t
+        lo += (31 - __clz(m)) * step;
+        hi = min(lo + step, hi);
+      }
+      cursor = lo;
+      if (lane == 0) {
+        const PassDesc& pd = g.passes[lo];
+        int go = 1;
         long it = 0;
-        while (ld_acquire(g.done + pd.dep) < need) {
-          if (++it > g.spin_limit || *(volatile unsigned*)g.abort) { go = 0; break; }
-          __nanosleep(100);
+        for (int k = 0; k < 2 && go; ++k) {
+          const int dep = k ? pd.dep2 : pd.dep;
+          if (dep < 0) continue;
+          const unsigned need = (unsigned)(k ? pd.need2 : pd.need);
+          while (ld_acquire(g.done + dep) < need) {
+            if (++it > g.spin_limit || *(volatile unsigned*)g.abort) { go = 0; break; }
+            __nanosleep(100);
+          }
         }
         if (!go) { atomicOr(g.err, ES_DEV_ERR_BATCH_TIMEOUT); atomicExch(g.abort, 1u); }
+        s_pass = lo;
+        s_go = go;
+        s_next = nxt;
       }
-      s_go = go;
     }
     __syncthreads();
     if (!s_go) break;
+    const PassDesc pd = g.passes[s_pass];
     const BoxDev& b = g.boxes[pd.box];
-    const int tile = (int)(t - (unsigned)pd.first);
+    const int t0 = (int)(t - (unsigned)pd.first) * g.chunk;
+    const int t1 = min(t0 + g.chunk, pd.tiles);
     switch (b.n) {
-#define ESB_CASE(NN) case NN: run_item<NN>(b, pd, tile, sm, sred); break;
+#define ESB_CASE(NN) case NN: run_chunk<NN>(b, pd, t0, t1, sm, sred); break;
       ESB_SIZES(ESB_CASE)
 #undef ESB_CASE
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(g.done + lo, 1u);
+    if (threadIdx.x == 0) {
+      atomicAdd(g.done + s_pass, 1u);
+      s_t = *(volatile unsigned*)g.abort ? g.total : s_next;
+    }
+    __syncthreads();
   }
 }
 
@@ -410,6 +695,7 @@ struct es_batch {
   void* base = nullptr;
   esb::BoxDev* d_boxes = nullptr;
   esb::PassDesc* d_passes = nullptr;
+  int* d_first = nullptr;
   unsigned* ctrl = nullptr;          // [0] ticket, [1] err, [2] abort, then done[npasses]
   int npasses = 0;
   unsigned total = 0;
@@ -417,8 +703,124 @@ struct es_batch {
   void* zero_base = nullptr;
   cudaGraphExec_t graph = nullptr;
   long spin_limit = esb::kSpinLimit;
+  int lanes = 0, chunk = 1;          // queue schedule (lanes 0: every box its own lane)
   std::vector<esb::PassDesc> h_passes;
+  std::vector<std::vector<esb::PassDesc>> per_box;   // dep / dep2: indices within the box's list
+  std::vector<int> h_n, h_nr;                        // HII_DIM and radius count per box
 };
+
+namespace {
+
+using PassList = std::vector<esb::PassDesc>;
+
+// One box's passes, dependencies as indices in the list: the filter table of every radius, the
+// forward transform (3 passes), per radius the z inverse, y inverse and row pass (and in sphere
+// mode, from radius 1 on, the painting of the centres its row pass found), the final step (with
+// delta_T), and with P(k) the forward transform of delta_T ending in the binning z pass.
+PassList box_passes(int box, int n, int nr, int update, int pk) {
+  int ctz, cty, rt, ft, sm;
+  size_info(n, &ctz, &cty, &rt, &ft, &sm);
+  const long k2n = 3L * (n / 2) * (n / 2) + 1;
+  PassList v;
+  auto add = [&](int op, int r, int tiles, int dep, int dep2) {
+    esb::PassDesc d;
+    std::memset(&d, 0, sizeof(d));
+    d.box = box; d.op = op; d.radius = r; d.tiles = tiles; d.dep = dep; d.dep2 = dep2;
+    v.push_back(d);
+    return (int)v.size() - 1;
+  };
+  const int iw = add(esb::B_WTAB, 0, (int)((nr * k2n + esb::WTAB_TILE - 1) / esb::WTAB_TILE), -1, -1);
+  const int ir2c = add(esb::B_ROW_R2C, 0, rt, -1, -1);
+  const int iyf = add(esb::B_COL_Y_FWD, 0, cty, ir2c, -1);
+  const int izf = add(esb::B_COL_Z_FWD, 0, ctz, iyf, -1);
+  std::vector<int> irow(nr), ipaint(nr, -1);
+  for (int r = 0; r < nr; ++r) {
+    // the z inverse writes the spectrum buffer of its parity, last read by radius r - 2's row pass
+    const int iz = add(esb::B_COL_Z_INV, r, ctz, r < 2 ? izf : irow[r - 2], r < 2 ? iw : -1);
+    const int iy = add(esb::B_COL_Y_INV, r, cty, iz, -1);
+    // the row pass needs its spectrum and radius r - 1's statistics and delta_R; in sphere mode
+    // it refills the centre list, which radius r - 1's painting must have finished reading
+    irow[r] = add(esb::B_ROW_C2R, r, rt, iy, r == 0 ? -1 : (ipaint[r - 1] >= 0 ? ipaint[r - 1] : irow[r - 1]));
+    if (update && r >= 1) ipaint[r] = add(esb::B_PAINT, r, esb::PAINT_TILES, irow[r], -1);
+  }
+  const int ifin = add(esb::B_FINAL, 0, ft, ipaint[nr - 1] >= 0 ? ipaint[nr - 1] : irow[nr - 1], -1);
+  if (pk) {
+    // P(k) of delta_T (written by the final step) through the forward spectrum's buffers
+    const int ipr = add(esb::B_PK_R2C, 0, rt, ifin, -1);
+    const int ipy = add(esb::B_COL_Y_FWD, 0, cty, ipr, -1);
+    add(esb::B_COL_Z_FWD_PK, 0, ctz, ipy, -1);
+  }
+  return v;
+}
+
+// Merge the boxes' pass lists into the work queue (see the top of the file) and fill in tickets
+// and global dependency indices; returns the number of tickets.
+unsigned make_queue(const std::vector<PassList>& per_box, const std::vector<int>& n, const std::vector<int>& nr,
+                    int lanes, int chunk, PassList* out) {
+  const int count = (int)per_box.size();
+  const int L = lanes <= 0 || lanes > count ? count : lanes;
+  // deal boxes to lanes, heaviest (N^3 * N_R) first onto the lightest lane
+  std::vector<double> cost(count);
+  for (int i = 0; i < count; ++i) cost[i] = std::pow((double)n[i], 3) * nr[i];
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<std::vector<int>> lane_boxes(L);
+  std::vector<double> load(L, 0.0);
+  for (int i : order) {
+    int best = 0;
+    for (int l = 1; l < L; ++l) if (load[l] < load[best]) best = l;
+    lane_boxes[best].push_back(i);
+    load[best] += cost[i];
+  }
+  // lanes advance in proportion to work: always extend the lane with the least work queued
+  struct Cursor { size_t box = 0, pass = 0; double work = 0.0; };
+  std::vector<Cursor> cur(L);
+  std::vector<std::vector<int>> gidx(count);
+  for (int i = 0; i < count; ++i) gidx[i].assign(per_box[i].size(), -1);
+  PassList& q = *out;
+  q.clear();
+  unsigned first = 0;
+  for (;;) {
+    int pick = -1;
+    for (int l = 0; l < L; ++l)
+      if (cur[l].box < lane_boxes[l].size() && (pick < 0 || cur[l].work < cur[pick].work)) pick = l;
+    if (pick < 0) break;
+    Cursor& c = cur[pick];
+    const int box = lane_boxes[pick][c.box];
+    esb::PassDesc d = per_box[box][c.pass];
+    const int ld = d.dep, ld2 = d.dep2;
+    d.dep = ld >= 0 ? gidx[box][ld] : -1;
+    d.dep2 = ld2 >= 0 ? gidx[box][ld2] : -1;
+    d.need = d.dep >= 0 ? q[d.dep].tickets : 0;
+    d.need2 = d.dep2 >= 0 ? q[d.dep2].tickets : 0;
+    d.tickets = (d.tiles + chunk - 1) / chunk;
+    d.first = (int)first;
+    first += (unsigned)d.tickets;
+    gidx[box][c.pass] = (int)q.size();
+    q.push_back(d);
+    c.work += std::pow((double)n[box], 3);
+    if (++c.pass == per_box[box].size()) { c.pass = 0; ++c.box; }
+  }
+  return first;
+}
+
+cudaError_t upload_queue(es_batch* bt) {
+  std::vector<int> first(bt->h_passes.size());
+  for (size_t k = 0; k < first.size(); ++k) first[k] = bt->h_passes[k].first;
+  cudaError_t e = cudaMemcpy(bt->d_passes, bt->h_passes.data(), sizeof(esb::PassDesc) * bt->h_passes.size(),
+                             cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(bt->d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice);
+  return e;
+}
+
+void build_queue(es_batch* bt, int lanes, int chunk) {
+  bt->total = make_queue(bt->per_box, bt->h_n, bt->h_nr, lanes, chunk, &bt->h_passes);
+  bt->lanes = lanes <= 0 || lanes > bt->count ? 0 : lanes;
+  bt->chunk = chunk;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -430,13 +832,12 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
   if (cudaGetDevice(&bt->device) != cudaSuccess) return cleanup(bfail(ES_E_CUDA, "no CUDA device"));
   bt->count = count;
   std::vector<esb::BoxDev> hb(count);
-  std::vector<esb::PassDesc> passes;
   // sizes of every box's workspace
-  struct Sz { size_t X, Xn, T, Tn, dR, flags, stats, partials, arrive, rad, tw; };
+  struct Sz { size_t X, Xn, T, Tn, dR, flags, stats, partials, arrive, rad, tw, wtab, centers, ccount, pk_part,
+               partials2, thr; };
   std::vector<Sz> sz(count);
   size_t total_bytes = 0;
   int smem = 0;
-  std::vector<std::vector<int>> levels(count);
   for (int i = 0; i < count; ++i) {
     const es_batch_box& bx = boxes[i];
     int ctz, cty, rt, ft, sm;
@@ -445,56 +846,51 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
     const es_ionize_params& p = bx.params;
     if (!bx.delta || !bx.out || !bx.nf || !p.radii || p.n_radii < 1 || p.n_radii > 4096)
       return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d has a NULL buffer or bad radius count", i));
-    if (p.update != 0) return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d: the batched engine paints centres only (update=0)", i));
-    if (!(p.zeta > 0) || p.filter_type < 0 || p.filter_type > 2)
+    if (!(p.zeta > 0) || p.filter_type < 0 || p.filter_type > 2 || p.update < 0 || p.update > 1)
       return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d has bad parameters", i));
+    const bool want_dt = bx.t_factor != 0.f, want_pk = want_dt && bx.k2_thresholds;
+    if (want_dt && (!bx.dT || !bx.ave))
+      return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d: delta_T needs dT and ave buffers", i));
+    if (want_pk) {
+      if (!bx.pk || bx.nbins < 1 || bx.nbins > es::PK_MAX_BINS)
+        return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d: P(k) needs pk and 1..%d bins", i, es::PK_MAX_BINS));
+      for (int k = 1; k < bx.nbins; ++k)
+        if (bx.k2_thresholds[k] < bx.k2_thresholds[k - 1])
+          return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d: k^2 thresholds must be non-decreasing", i));
+    }
+    if (want_pk) sm += esb::PK_SMEM;
     smem = sm > smem ? sm : smem;
     const size_t N = bx.n, M = N / 2;
     Sz& s = sz[i];
-    s.X = a256(N * N * M * 8); s.Xn = a256(N * N * 8); s.T = s.X; s.Tn = s.Xn;
+    s.X = a256(N * N * M * 8); s.Xn = a256(N * N * 8); s.T = 2 * s.X; s.Tn = 2 * s.Xn;
     s.dR = a256(N * N * N * 4); s.flags = a256(N * N * N / 8); s.stats = a256((size_t)p.n_radii * 16);
-    s.partials = a256((size_t)(rt > ft ? rt : ft) * 4); s.arrive = a256((size_t)(p.n_radii + 1) * 4);
+    s.partials = a256((size_t)(rt > ft ? rt : ft) * 4); s.arrive = a256((size_t)(p.n_radii + 3) * 4);
     s.rad = a256((size_t)p.n_radii * sizeof(esb::RadB)); s.tw = a256(N * 8);
-    total_bytes += s.X + s.Xn + s.T + s.Tn + 2 * s.dR + s.flags + s.stats + s.partials + s.arrive + s.rad + s.tw;
+    s.wtab = a256((size_t)p.n_radii * (3 * M * M + 1) * 4);
+    s.centers = p.update ? a256(N * N * N * 4) : 0;
+    s.ccount = a256((size_t)p.n_radii * 4);
+    s.pk_part = want_pk ? a256((size_t)ctz * 3 * bx.nbins * 4) : 0;
+    s.thr = want_pk ? a256((size_t)bx.nbins * 4) : 0;
+    s.partials2 = want_dt ? a256((size_t)ft * 4) : 0;
+    total_bytes += s.X + s.Xn + s.T + s.Tn + 2 * s.dR + s.flags + s.stats + s.partials + s.arrive + s.rad + s.tw +
+                   s.wtab + s.centers + s.ccount + s.pk_part + s.thr + s.partials2;
   }
-  // passes, interleaved by level: forward (3), 3 per radius, final
-  std::vector<std::vector<esb::PassDesc>> per_box(count);
+  bt->per_box.assign(count, {});
+  bt->h_n.assign(count, 0);
+  bt->h_nr.assign(count, 0);
   for (int i = 0; i < count; ++i) {
-    int ctz, cty, rt, ft, sm;
-    size_info(boxes[i].n, &ctz, &cty, &rt, &ft, &sm);
-    auto& v = per_box[i];
-    v.push_back({i, esb::B_ROW_R2C, 0, rt, 0, -1, 0, 0});
-    v.push_back({i, esb::B_COL_Y_FWD, 0, cty, 0, -1, 0, 0});
-    v.push_back({i, esb::B_COL_Z_FWD, 0, ctz, 0, -1, 0, 0});
-    for (int r = 0; r < boxes[i].params.n_radii; ++r) {
-      v.push_back({i, esb::B_COL_Z_INV, r, ctz, 0, -1, 0, 0});
-      v.push_back({i, esb::B_COL_Y_INV, r, cty, 0, -1, 0, 0});
-      v.push_back({i, esb::B_ROW_C2R, r, rt, 0, -1, 0, 0});
-    }
-    v.push_back({i, esb::B_FINAL, 0, ft, 0, -1, 0, 0});
+    bt->h_n[i] = boxes[i].n;
+    bt->h_nr[i] = boxes[i].params.n_radii;
+    bt->per_box[i] = box_passes(i, boxes[i].n, boxes[i].params.n_radii, boxes[i].params.update,
+                                boxes[i].t_factor != 0.f && boxes[i].k2_thresholds ? 1 : 0);
   }
-  size_t max_levels = 0;
-  for (auto& v : per_box) max_levels = v.size() > max_levels ? v.size() : max_levels;
-  std::vector<int> last(count, -1);
-  unsigned first = 0;
-  for (size_t l = 0; l < max_levels; ++l)
-    for (int i = 0; i < count; ++i) {
-      if (l >= per_box[i].size()) continue;
-      esb::PassDesc d = per_box[i][l];
-      d.first = (int)first;
-      d.dep = last[i];
-      d.need = last[i] >= 0 ? passes[last[i]].tiles : 0;
-      first += d.tiles;
-      last[i] = (int)passes.size();
-      passes.push_back(d);
-    }
-  bt->npasses = (int)passes.size();
-  bt->h_passes = passes;
-  bt->total = first;
+  build_queue(bt, 0, 8);
+  bt->npasses = (int)bt->h_passes.size();
   bt->smem = smem;
-  const size_t ctrl_bytes = a256((3 + passes.size()) * 4);
-  const size_t box_bytes = a256(count * sizeof(esb::BoxDev)), pass_bytes = a256(passes.size() * sizeof(esb::PassDesc));
-  total_bytes += ctrl_bytes + box_bytes + pass_bytes;
+  const size_t ctrl_bytes = a256((3 + bt->h_passes.size()) * 4);
+  const size_t box_bytes = a256(count * sizeof(esb::BoxDev)), pass_bytes = a256(bt->h_passes.size() * sizeof(esb::PassDesc));
+  const size_t first_bytes = a256(bt->h_passes.size() * sizeof(int));
+  total_bytes += ctrl_bytes + box_bytes + pass_bytes + first_bytes;
   if (cudaMalloc(&bt->base, total_bytes) != cudaSuccess) {
     cudaGetLastError();
     return cleanup(bfail(ES_E_NOMEM, "es_batch_create: cannot allocate %zu bytes", total_bytes));
@@ -505,11 +901,16 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
   bt->ctrl = reinterpret_cast<unsigned*>(b);
   off += ctrl_bytes;
   bt->zero_base = b;
-  std::vector<size_t> flags_off(count), arrive_off(count);
-  for (int i = 0; i < count; ++i) { flags_off[i] = off; off += sz[i].flags; arrive_off[i] = off; off += sz[i].arrive; }
+  std::vector<size_t> flags_off(count), arrive_off(count), ccount_off(count);
+  for (int i = 0; i < count; ++i) {
+    flags_off[i] = off; off += sz[i].flags;
+    arrive_off[i] = off; off += sz[i].arrive;
+    ccount_off[i] = off; off += sz[i].ccount;
+  }
   bt->zero_bytes = off;
   bt->d_boxes = reinterpret_cast<esb::BoxDev*>(b + off); off += box_bytes;
   bt->d_passes = reinterpret_cast<esb::PassDesc*>(b + off); off += pass_bytes;
+  bt->d_first = reinterpret_cast<int*>(b + off); off += first_bytes;
   for (int i = 0; i < count; ++i) {
     const es_batch_box& bx = boxes[i];
     const es_ionize_params& p = bx.params;
@@ -524,12 +925,32 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
     d.delta = bx.delta; d.out = bx.out; d.nf = bx.nf;
     d.X = reinterpret_cast<float2*>(b + off); off += s.X;
     d.Xnyq = reinterpret_cast<float2*>(b + off); off += s.Xn;
-    d.T = reinterpret_cast<float2*>(b + off); off += s.T;
-    d.Tnyq = reinterpret_cast<float2*>(b + off); off += s.Tn;
+    for (int h = 0; h < 2; ++h) {
+      d.T[h] = reinterpret_cast<float2*>(b + off); off += s.T / 2;
+      d.Tnyq[h] = reinterpret_cast<float2*>(b + off); off += s.Tn / 2;
+    }
     d.dR0 = reinterpret_cast<float*>(b + off); off += s.dR;
     d.dR1 = reinterpret_cast<float*>(b + off); off += s.dR;
     d.flags = reinterpret_cast<unsigned long long*>(b + flags_off[i]);
     d.arrive = reinterpret_cast<unsigned*>(b + arrive_off[i]);
+    d.ccount = reinterpret_cast<unsigned*>(b + ccount_off[i]);
+    d.update = p.update;
+    d.k2n = 3 * (bx.n / 2) * (bx.n / 2) + 1;
+    d.wtab = reinterpret_cast<float*>(b + off); off += s.wtab;
+    d.centers = s.centers ? reinterpret_cast<uint32_t*>(b + off) : nullptr; off += s.centers;
+    d.tfac = bx.t_factor;
+    d.dT = bx.dT; d.ave = bx.ave;
+    d.pk_norm = (float)(bx.box_len * bx.box_len * bx.box_len / ((double)bx.n * bx.n * bx.n));
+    d.volume = (float)(bx.box_len * bx.box_len * bx.box_len);
+    d.dimensional = bx.dimensional;
+    d.nbins = s.thr ? bx.nbins : 0;
+    d.pk_out = s.thr ? bx.pk : nullptr;
+    d.pk_part = s.pk_part ? reinterpret_cast<float*>(b + off) : nullptr; off += s.pk_part;
+    d.partials2 = s.partials2 ? reinterpret_cast<float*>(b + off) : nullptr; off += s.partials2;
+    int* thr = s.thr ? reinterpret_cast<int*>(b + off) : nullptr; off += s.thr;
+    d.thr = thr;
+    if (thr && cudaMemcpy(thr, bx.k2_thresholds, sizeof(int) * bx.nbins, cudaMemcpyHostToDevice) != cudaSuccess)
+      return cleanup(bfail(ES_E_CUDA, "es_batch_create: upload failed"));
     d.stats = reinterpret_cast<float*>(b + off); off += s.stats;
     d.partials = reinterpret_cast<float*>(b + off); off += s.partials;
     esb::RadB* rad = reinterpret_cast<esb::RadB*>(b + off); off += s.rad;
@@ -539,7 +960,20 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
     for (int r = 0; r < p.n_radii; ++r) {
       const float R = p.radii[r].R, den = p.radii[r].denom;
       if (!(R > 0) || !(den > 0)) return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d radius %d invalid", i, r));
-      hr[r].R = R; hr[r].denom = den; hr[r].pad = 0;
+      hr[r].R = R; hr[r].denom = den;
+      // sphere: cells with integer |d|^2 < R_cells^2 (find_bubbles.cu:97-98); in the reference's
+      // mode R in Mpc is used as cells with a float32 compare
+      if (p.ref_compat) {
+        const float r2 = R * R;
+        long m = (long)std::floor((double)r2);
+        while (m >= 0 && (float)m >= r2) --m;
+        hr[r].r2max = (int)m;
+      } else {
+        const double rc2 = std::pow((double)R / (bx.box_len / bx.n), 2);
+        long m = (long)std::floor(rc2);
+        while (m >= 0 && (double)m >= rc2) --m;
+        hr[r].r2max = (int)m;
+      }
       hr[r].k2cut = 0x7fffffff;
       if (p.filter_type == 1 || (p.ref_compat && p.filter_type == 0)) {
         const double dk = d.dk;
@@ -559,7 +993,7 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
       return cleanup(bfail(ES_E_CUDA, "es_batch_create: upload failed"));
   }
   if (cudaMemcpy(bt->d_boxes, hb.data(), sizeof(esb::BoxDev) * count, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(bt->d_passes, passes.data(), sizeof(esb::PassDesc) * passes.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      upload_queue(bt) != cudaSuccess)
     return cleanup(bfail(ES_E_CUDA, "es_batch_create: upload failed"));
   // persistent grid: exactly the co-resident CTAs (the queue relies on all CTAs being resident)
   if (cudaFuncSetAttribute(esb::batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
@@ -578,6 +1012,7 @@ static int batch_enqueue(es_batch* bt, cudaStream_t s) {
   esb::BatchArgs g;
   g.boxes = bt->d_boxes;
   g.passes = bt->d_passes;
+  g.first = bt->d_first;
   g.npasses = bt->npasses;
   g.total = bt->total;
   g.ticket = bt->ctrl;
@@ -585,6 +1020,7 @@ static int batch_enqueue(es_batch* bt, cudaStream_t s) {
   g.abort = bt->ctrl + 2;
   g.done = bt->ctrl + 3;
   g.spin_limit = bt->spin_limit;
+  g.chunk = bt->chunk;
   esb::batch_kernel<<<bt->grid, esb::BT, bt->smem, s>>>(g);
   ESB_CUDA(cudaGetLastError());
   return ES_OK;
@@ -628,6 +1064,45 @@ int es_batch_debug_stall(es_batch* bt, int pass, long spin_limit) {
   return ES_OK;
 }
 
+int es_batch_queue(const int* n, const int* n_radii, const int* update, const int* pk, int count, int lanes,
+                   int chunk, int* out, int cap) {
+  if (!n || !n_radii || count <= 0 || lanes < 0 || chunk < 1 || chunk > 64 || (!out && cap > 0))
+    return bfail(ES_E_ARG, "es_batch_queue: bad arguments");
+  std::vector<PassList> per_box(count);
+  std::vector<int> vn(n, n + count), vr(n_radii, n_radii + count);
+  for (int i = 0; i < count; ++i) {
+    int a, b2, c, d, e;
+    if (!size_info(n[i], &a, &b2, &c, &d, &e)) return bfail(ES_E_UNSUPPORTED, "es_batch_queue: HII_DIM=%d", n[i]);
+    if (n_radii[i] < 1 || n_radii[i] > 4096) return bfail(ES_E_ARG, "es_batch_queue: bad radius count");
+    per_box[i] = box_passes(i, n[i], n_radii[i], update ? update[i] : 0, pk ? pk[i] : 0);
+  }
+  PassList q;
+  make_queue(per_box, vn, vr, lanes, chunk, &q);
+  for (size_t k = 0; k < q.size() && (int)k < cap; ++k) {
+    const esb::PassDesc& d = q[k];
+    const int row[8] = {d.box, d.op, d.radius, d.tiles, d.first, d.tickets, d.dep, d.dep2};
+    std::memcpy(out + 8 * k, row, sizeof(row));
+  }
+  return (int)q.size();
+}
+
+int es_batch_set_schedule(es_batch* bt, int lanes, int chunk) {
+  if (!bt || lanes < 0 || chunk < 1 || chunk > 64) return bfail(ES_E_ARG, "es_batch_set_schedule: bad arguments");
+  build_queue(bt, lanes, chunk);
+  ESB_CUDA(upload_queue(bt));
+  bt->spin_limit = esb::kSpinLimit;
+  if (bt->graph) { cudaGraphExecDestroy(bt->graph); bt->graph = nullptr; }
+  return ES_OK;
+}
+
+int es_batch_get_schedule(const es_batch* bt, int* lanes, int* chunk, unsigned* tickets) {
+  if (!bt) return bfail(ES_E_ARG, "es_batch_get_schedule: NULL batch");
+  if (lanes) *lanes = bt->lanes;
+  if (chunk) *chunk = bt->chunk;
+  if (tickets) *tickets = bt->total;
+  return ES_OK;
+}
+
 int es_batch_check(es_batch* bt, void* stream) {
   if (!bt) return bfail(ES_E_ARG, "es_batch_check: NULL batch");
   unsigned w[2] = {0, 0};
@@ -641,7 +1116,11 @@ int es_batch_info(const es_batch* bt, int* grid, int* passes, unsigned* tiles, i
   if (!bt) return bfail(ES_E_ARG, "es_batch_info: NULL batch");
   if (grid) *grid = bt->grid;
   if (passes) *passes = bt->npasses;
-  if (tiles) *tiles = bt->total;
+  if (tiles) {
+    unsigned long long t = 0;
+    for (const auto& d : bt->h_passes) t += (unsigned)d.tiles;
+    *tiles = (unsigned)t;
+  }
   if (smem) *smem = bt->smem;
   return ES_OK;
 }

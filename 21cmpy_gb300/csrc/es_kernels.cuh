@@ -264,6 +264,65 @@ __device__ __forceinline__ float filter_weight(int k2, float dk, float R, int k2
   return W;
 }
 
+__device__ __forceinline__ int isqrt_dev(int v) {
+  int r = (int)sqrtf((float)v);
+  while (r * r > v) --r;
+  while ((r + 1) * (r + 1) <= v) ++r;
+  return r;
+}
+
+__device__ __forceinline__ unsigned long long bit_range(long lo, long hi, long q) {
+  // bits lo - 32q .. hi - 32q of a 32-bit half, clipped to [0, 31]; 0 when empty
+  if (lo < 32 * q) lo = 32 * q;
+  if (hi > 32 * q + 31) hi = 32 * q + 31;
+  if (lo > hi) return 0ull;
+  const int l = (int)(lo - 32 * q), h = (int)(hi - 32 * q);
+  const unsigned long long top = h == 31 ? 0xffffffffull : ((1ull << (h + 1)) - 1ull);
+  return top & ~((1ull << l) - 1ull);
+}
+
+// set voxels a..b (inclusive) in the pair-major bitmap: voxel v = 2p + h is bit (p % 32) + 32 h
+// of 64-bit word p / 32
+__device__ __forceinline__ void set_bits(uint32_t* flags, long a, long b) {
+  unsigned long long* f = reinterpret_cast<unsigned long long*>(flags);
+  const long e_lo = (a + 1) >> 1, e_hi = b >> 1;          // even voxels 2p in [a, b]
+  const long o_lo = a >> 1, o_hi = (b - 1) >> 1;          // odd voxels 2p + 1 in [a, b]
+  for (long q = (a >> 1) / 32; q <= (b >> 1) / 32; ++q) {
+    const unsigned long long m = bit_range(e_lo, e_hi, q) | (bit_range(o_lo, o_hi, q) << 32);
+    if (m) atomicOr(f + q, m);
+  }
+}
+
+
+// Sphere painting (update_sphere_kernel, find_bubbles.cu:73-102), one warp per centre: every cell
+// within integer |d|^2 <= r2max of voxel v (linear index, x fastest) is set in the pair-major
+// bitmap; lanes split the (dz, dy) rows of the ball; periodic wraps, otherwise clips to the box.
+__device__ __forceinline__ void paint_ball(uint32_t v, int n, int r2max, int periodic, uint32_t* flags) {
+  const int lane = threadIdx.x & 31;
+  const int r = isqrt_dev(r2max), side = 2 * r + 1;
+  const int cx = (int)(v % n), cy = (int)((v / n) % n), cz = (int)(v / ((uint32_t)n * n));
+  for (int idx = lane; idx < side * side; idx += 32) {
+    const int dz = idx / side - r, dy = idx % side - r;
+    const int rem = r2max - dz * dz - dy * dy;
+    if (rem < 0) continue;
+    const int w = isqrt_dev(rem);
+    int z = cz + dz, y = cy + dy;
+    if (periodic) { z = ((z % n) + n) % n; y = ((y % n) + n) % n; }
+    else if (z < 0 || z >= n || y < 0 || y >= n) continue;
+    const long rb = ((long)z * n + y) * n;
+    int x0 = cx - w, x1 = cx + w;
+    if (periodic) {
+      if (x1 - x0 + 1 >= n) { set_bits(flags, rb, rb + n - 1); continue; }
+      if (x0 < 0) { set_bits(flags, rb + x0 + n, rb + n - 1); x0 = 0; }
+      if (x1 >= n) { set_bits(flags, rb, rb + x1 - n); x1 = n - 1; }
+    } else {
+      if (x0 < 0) x0 = 0;
+      if (x1 > n - 1) x1 = n - 1;
+    }
+    set_bits(flags, rb + x0, rb + x1);
+  }
+}
+
 template <int N> __device__ __forceinline__ int wrap2(int k) {
   const int w = (k > N / 2) ? k - N : k;
   return w * w;

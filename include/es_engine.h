@@ -180,13 +180,15 @@ int es_profile_read(es_plan* plan, float* total_ms, int* counts, int nops);
 
 /* Batched form (no counterpart in the reference, whose boxes run one at a time): many boxes of
  * uneven HII_DIM (32..256), each with its own parameters, run in ONE persistent launch.  The
- * host lists every box's passes (forward transform, three passes per radius, final step) level by
- * level, interleaving boxes; CTAs take tiles from a global ticket counter in that order and start
- * a pass once the box's previous pass has finished (bounded waits; a timeout aborts the launch and
- * es_batch_check reports ES_E_DEVICE).  Centre-pixel updates only.  delta / out / nf are device
- * buffers owned by the caller; es_batch_create copies the parameters and allocates the
- * workspace of every box.  es_batch_run(use_graph = 1) captures the clear + launch into a CUDA
- * graph on its first call and replays it afterwards. */
+ * host lists every box's passes (forward transform, three passes per radius, final step) and
+ * merges them into a work queue: boxes are dealt to lanes balanced by N^3 * N_R, the lanes
+ * advance side by side in proportion to work, and CTAs take tickets of `chunk` tiles from a
+ * global counter in queue order.  A pass starts once its dependencies (earlier passes of its box)
+ * have finished (bounded waits; a timeout aborts the launch and es_batch_check reports
+ * ES_E_DEVICE).  Centre-pixel (update 0) and sphere (update 1) modes.  delta / out / nf are
+ * device buffers owned by the caller; es_batch_create copies the parameters and allocates the workspace of every box.
+ * es_batch_run(use_graph = 1) captures the clear + launch into a CUDA graph on its first call and
+ * replays it afterwards. */
 typedef struct es_batch es_batch;
 typedef struct es_batch_box {
   int n;                      /* HII_DIM */
@@ -194,12 +196,34 @@ typedef struct es_batch_box {
   const float* delta;         /* device float32 n^3 density */
   float* out;                 /* device float32 n^3 output (x_HI or ionised fraction) */
   float* nf;                  /* device float: mean x_HI */
-  es_ionize_params params;    /* as for es_ionize (update must be 0) */
+  es_ionize_params params;    /* as for es_ionize */
+  /* Optional 21-cm products of the box (delta_T.py:73-98), as es_delta_T and
+   * es_power_spectrum compute them: t_factor = 0 skips both; k2_thresholds = NULL skips P(k). */
+  float t_factor;             /* brightness-temperature factor c(z) [mK] */
+  float* dT;                  /* device float n^3: delta_T = c x_HI (1 + delta) */
+  float* ave;                 /* device float: mean delta_T */
+  const int* k2_thresholds;   /* host int[nbins], non-decreasing: P(k) bins as es_power_spectrum */
+  int nbins;                  /* 1..128 */
+  int dimensional;            /* 1: P(k) of delta_T - ave instead of delta_T / ave - 1 */
+  float* pk;                  /* device float[3 * nbins]: mean k^3 |g|^2 / (2 pi^2 V), mean |k|, count */
 } es_batch_box;
 int es_batch_create(const es_batch_box* boxes, int count, es_batch** batch);
 int es_batch_run(es_batch* batch, int use_graph, void* stream);
 int es_batch_check(es_batch* batch, void* stream);
 int es_batch_info(const es_batch* batch, int* grid, int* passes, unsigned* tiles, int* smem);
+/* Queue schedule: `lanes` boxes in flight (0 = every box its own lane, the default), `chunk`
+ * tiles per ticket (1..64, default 8).  Rebuilds the queue; the next es_batch_run recaptures. */
+int es_batch_set_schedule(es_batch* batch, int lanes, int chunk);
+int es_batch_get_schedule(const es_batch* batch, int* lanes, int* chunk, unsigned* tickets);
+/* The work queue es_batch_create would build for boxes of HII_DIM n[i] with n_radii[i] radii and
+ * update mode update[i] (NULL: all 0) under a schedule, computed on the host (no device needed):
+ * per pass 8 ints (box, op, radius, tiles, first ticket, tickets, dependency, second dependency;
+ * -1 = none) into out[8 * cap].  op: 0 row r2c, 1 y forward, 2 z forward, 3 z inverse, 4 y
+ * inverse, 5 row c2r, 6 final, 7 filter tables, 8 sphere painting, 9 row r2c of delta_T, 10 z
+ * forward + P(k) binning.  pk (NULL: none) flags the boxes with delta_T and P(k).  Returns the
+ * number of passes, or a negative error code. */
+int es_batch_queue(const int* n, const int* n_radii, const int* update, const int* pk, int count, int lanes,
+                   int chunk, int* out, int cap);
 int es_batch_destroy(es_batch* batch);
 /* Failure-detection test hook: pass `pass` waits for one tile more than its dependency
  * completes and every wait gives up after spin_limit polls of ~100 ns.  The launch then aborts

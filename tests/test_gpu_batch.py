@@ -26,12 +26,15 @@ def mods():
     return module("engine"), module("batch")
 
 
-def _boxes(specs):
+def _boxes(specs, **kw):
     out = []
-    for n, seed, z, zeta, rmax, tvir in specs:
+    for n, seed, z, zeta, rmax, tvir, *extra in specs:
         L = 1.5 * n
         d = torch.from_numpy(grf.density_box(n, L, seed, z)).cuda()
-        st = sch.ionize_setup(n, L, z, zeta=zeta, t_vir_min=tvir, R_max=rmax, cosmo=cos.BASELINE_COSMO)
+        args = dict(kw)
+        if extra:
+            args.update(extra[0])
+        st = sch.ionize_setup(n, L, z, zeta=zeta, t_vir_min=tvir, R_max=rmax, cosmo=cos.BASELINE_COSMO, **args)
         out.append((d, st))
     return out
 
@@ -50,7 +53,7 @@ def test_batch_matches_per_box_engine_and_oracle(mods):
         outs = [o.clone() for o in outs]
         nf = nf.clone()
         info = b.info()
-    assert info["passes"] == sum(4 + 3 * st.n_radii for _, st in boxes)
+    assert info["passes"] == sum(5 + 3 * st.n_radii for _, st in boxes)
     for i, (d, st) in enumerate(boxes):
         with eng.ExcursionSetPlan(st.n, st.box_len) as p:
             xh, nfp = p.run(d, st)
@@ -65,6 +68,79 @@ def test_batch_matches_per_box_engine_and_oracle(mods):
         assert bad.sum() == 0, i
 
 
+SPHERE_SPECS = [(64, 11, 8.0, 30.0, 10.0, 1e4, dict(update=1)), (48, 12, 7.5, 50.0, 20.0, 2e4),
+                (96, 13, 8.5, 40.0, 15.0, 1e4, dict(update=1)),
+                (64, 14, 8.0, 30.0, 8.0, 1e4, dict(update=1, ref_compat=True)),
+                (32, 15, 9.0, 60.0, 30.0, 3e4, dict(update=1, filter_type=2))]
+
+
+def test_batch_sphere_painting_matches_per_box_engine(mods):
+    # sphere mode (find_bubbles.cu:73-140) in the persistent launch, mixed with a centre-mode box:
+    # the row pass lists the centres, a painting pass per radius marks their balls
+    eng, batch = mods
+    boxes = _boxes(SPHERE_SPECS)
+    assert [st.update for _, st in boxes] == [1, 0, 1, 1, 1]
+    with batch.BatchedExcursionSet(boxes, use_graph=True, lanes=2, chunk=4) as b:
+        outs, nf = b.run()
+        b.check()
+        outs = [o.clone() for o in outs]
+        nf = nf.clone()
+        info = b.info()
+    assert info["passes"] == sum(5 + 3 * st.n_radii + (st.n_radii - 1 if st.update else 0) for _, st in boxes)
+    for i, (d, st) in enumerate(boxes):
+        with eng.ExcursionSetPlan(st.n, st.box_len) as p:
+            xh, nfp = p.run(d, st)
+        diff = (outs[i] - xh).abs()
+        assert (diff > PARTIAL_ATOL).float().mean().item() <= 1e-5, (i, diff.max().item())
+        assert abs(nf[i].item() - nfp.item()) <= 1e-5, i
+    d, st = boxes[0]                       # one sphere box straight against the float64 oracle
+    ref = O.conv_bubbles(d.cpu().numpy(), st)
+    ion = 1.0 - outs[0].cpu().numpy().astype(np.float64)
+    bad = (np.abs(ion - ref["ionized"]) > PARTIAL_ATOL) & ~ref["exempt"]
+    assert bad.sum() == 0
+    assert ref["flags"].mean() > 0.02     # the painting does real work here
+
+
+def test_batch_delta_T_and_pk_match_per_box_plans(mods):
+    # delta_T (fused into the final step) and P(k) (delta_T's forward transform ending in the
+    # binning z pass) inside the persistent launch, for some boxes of a mixed batch, against the
+    # per-box plan's es_delta_T / es_power_spectrum and against the float64 oracle's P(k)
+    eng, batch = mods
+    boxes = _boxes(SPECS[:4] + SPHERE_SPECS[:1])
+    facs = [cos.brightness_temperature_factor(st.z, cos.BASELINE_COSMO) for _, st in boxes]
+    edges = [sch.pk_edges(st.n, st.box_len, 12 + i) for i, (_, st) in enumerate(boxes)]
+    with batch.BatchedExcursionSet(boxes, use_graph=True, lanes=3, chunk=4, t_factors=facs, pk_edges=edges) as b:
+        outs, nf = b.run()
+        b.check()
+        outs = [o.clone() for o in outs]
+        dT = [t.clone() for t in b.dT]
+        ave = b.ave.clone()
+        pk = [q.cpu().numpy() for q in b.pk]
+        b.run()                                  # a replay gives the same products
+        b.check()
+        assert all(torch.equal(x, y) for x, y in zip(dT, b.dT)) and torch.equal(ave, b.ave)
+        assert all(np.array_equal(x, y.cpu().numpy()) for x, y in zip(pk, b.pk))
+    for i, (d, st) in enumerate(boxes):
+        with eng.ExcursionSetPlan(st.n, st.box_len) as p:
+            xh, _ = p.run(d, st)
+            t, a = p.delta_T(xh, d, facs[i])
+            q = p.power_spectrum(t, a, edges[i]).cpu().numpy()
+        # delta_T is c x_HI (1 + delta) of the batch's own x_HI, and close to the plan's
+        own = np.float32(facs[i]) * outs[i].cpu().numpy() * (np.float32(1) + d.cpu().numpy())
+        assert np.allclose(dT[i].cpu().numpy(), own, rtol=1e-6, atol=0), i
+        assert ((dT[i] - t).abs() > PARTIAL_ATOL * abs(facs[i]) * 2).float().mean().item() <= 1e-5, i
+        assert abs(ave[i].item() - a.item()) <= 1e-5 * abs(a.item()), i
+        assert np.array_equal(pk[i][2], q[2]), i          # exact mode counts
+        nz = q[2] > 0
+        assert np.allclose(pk[i][1][nz], q[1][nz], rtol=1e-5), i
+        assert (np.abs(pk[i][0][nz] - q[0][nz]) / np.abs(q[0][nz])).max() <= 1e-4, i
+    # one box's P(k) against the float64 oracle on the batch's own delta_T
+    from parity_util import compare_pk
+    d, st = boxes[1]
+    dT_o, ave_o = O.delta_T(outs[1].cpu().numpy().astype(np.float64), d.cpu().numpy(), facs[1])
+    compare_pk(pk[1], O.power_spectrum(dT_o, ave_o, st.box_len, edges[1]), "batch P(k)")
+
+
 def test_batch_graph_replay_is_deterministic(mods):
     _, batch = mods
     boxes = _boxes(SPECS[:4])
@@ -75,6 +151,34 @@ def test_batch_graph_replay_is_deterministic(mods):
         b.check()
         assert all(torch.equal(a, c) for a, c in zip(r1[0], o2))
         assert torch.equal(r1[1], n2)
+
+
+def test_batch_schedules_give_identical_results(mods):
+    # the queue order changes which CTA runs a tile and when, not what a tile computes or the
+    # fixed order of its reductions: every schedule gives the same bits
+    _, batch = mods
+    at = module("autotune")
+    boxes = _boxes(SPECS)
+    ref = None
+    with batch.BatchedExcursionSet(boxes, use_graph=True) as b:
+        for lanes, chunk in [(0, 1), (4, 1), (8, 2), (2, 4), (3, 64)]:
+            b.set_schedule(lanes, chunk)
+            assert b.schedule()["lanes"] == lanes and b.schedule()["chunk"] == chunk
+            outs, nf = b.run()
+            b.check()
+            got = [o.clone() for o in outs], nf.clone()
+            if ref is None:
+                ref = got
+            else:
+                assert all(torch.equal(a, c) for a, c in zip(ref[0], got[0])), (lanes, chunk)
+                assert torch.equal(ref[1], got[1])
+        times = at.tune_batch(b, schedules=[(0, 1), (4, 2)], repeats=1)
+        assert set(times) == {(0, 1), (4, 2)}
+        best = min(times, key=times.get)
+        assert (b.schedule()["lanes"], b.schedule()["chunk"]) == best
+        outs, nf = b.run()
+        b.check()
+        assert all(torch.equal(a, c) for a, c in zip(ref[0], outs))
 
 
 def test_batch_stalled_dependency_aborts_and_reports(mods):
