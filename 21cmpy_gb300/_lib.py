@@ -94,6 +94,8 @@ _PROTOS = {
     "es_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint),
                                 C.POINTER(C.c_int)]),
     "es_batch_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "es_batch_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "es_batch_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int]),
     "es_batch_get_schedule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint)]),
     "es_batch_queue": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                  C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int]),

@@ -155,7 +155,7 @@ def ensure_tuned(plan, allow_tuning: bool = True):
 
 
 # (lanes, tiles per ticket) of the persistent batched launch; lanes 0 = every box its own lane
-BATCH_SCHEDULES = [(0, 1), (4, 1), (8, 1), (16, 1), (8, 2), (16, 2), (8, 4), (16, 4), (32, 2)]
+BATCH_SCHEDULES = [(0, 8), (0, 16), (0, 4), (32, 8), (16, 8), (8, 16)]
 
 
 def tune_batch(b, schedules=BATCH_SCHEDULES, repeats: int = 3) -> dict:

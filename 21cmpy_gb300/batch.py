@@ -111,6 +111,22 @@ class BatchedExcursionSet:
         _lib.check("es_batch_set_schedule", self.lib.es_batch_set_schedule(self.handle, int(lanes), int(chunk)),
                    self.lib)
 
+    def profile(self, enable: bool = True):
+        """Clear and enable (or disable) the per-op cycle counters of the persistent launch."""
+        _lib.check("es_batch_profile", self.lib.es_batch_profile(self.handle, int(enable)), self.lib)
+
+    def profile_read(self) -> dict:
+        """Per op: SM clock cycles CTAs spent in its tiles, tiles, cycles finding and awaiting its
+        tickets, tickets (summed over the launches since ``profile(True)``)."""
+        buf = (C.c_ulonglong * (4 * len(OPS)))()
+        _lib.check("es_batch_profile_read", self.lib.es_batch_profile_read(self.handle, buf, len(OPS)), self.lib)
+        out = {}
+        for i, name in enumerate(OPS):
+            cyc, tiles, wait, tickets = (int(buf[4 * i + k]) for k in range(4))
+            if tiles:
+                out[name] = {"tile_cycles": cyc, "tiles": tiles, "wait_cycles": wait, "tickets": tickets}
+        return out
+
     def schedule(self) -> dict:
         lanes, chunk, tickets = C.c_int(), C.c_int(), C.c_uint()
         _lib.check("es_batch_get_schedule", self.lib.es_batch_get_schedule(

@@ -2,8 +2,8 @@
 // z) run in ONE persistent launch.  The host lists every box's passes (forward transform, three
 // passes per radius, final step) and merges them into one work queue: the boxes are dealt to
 // `lanes` lanes (balanced by N^3 * N_R), a lane runs its boxes one after the other, and the lanes
-// advance side by side in proportion to work done, so only `lanes` boxes' workspaces are live at a
-// time (they stay in L2 at these sizes).  CTAs take tickets of `chunk` tiles from a global counter
+// advance side by side, each in proportion to its own total work so that they finish together;
+// only `lanes` boxes' workspaces are live at a time.  CTAs take tickets of `chunk` tiles from a global counter
 // in queue order.  A pass waits until its dependencies (at most two earlier passes of its box)
 // have counted all their tickets done.  The filtered spectrum alternates between two buffers by
 // radius parity, so the z inverse of radius r + 1 depends only on the row pass of radius r - 1 and
@@ -33,10 +33,11 @@ constexpr unsigned ES_DEV_ERR_BATCH_TIMEOUT = 2u;
 enum BOp { B_ROW_R2C = 0, B_COL_Y_FWD = 1, B_COL_Z_FWD = 2, B_COL_Z_INV = 3, B_COL_Y_INV = 4, B_ROW_C2R = 5, B_FINAL = 6,
            B_WTAB = 7, B_PAINT = 8, B_PK_R2C = 9, B_COL_Z_FWD_PK = 10 };
 constexpr int WTAB_TILE = 2048;      // filter-table entries per tile
+constexpr int PROF_OPS = 16;         // per-op counters of the optional profile
 constexpr int PAINT_TILES = 64;      // tiles of a painting pass (8 warps each, one centre per warp at a time)
-// P(k) binning's shared memory after a column tile's buffers: per-warp bins [8][3][PK_MAX_BINS],
+// P(k) binning's shared memory after a column tile's buffers: per-warp bins [8][3][nbins],
 // per-warp scratch [8][32][4], the bin thresholds
-constexpr int PK_SMEM = (8 * 3 * PK_MAX_BINS + 8 * 32 * 4 + PK_MAX_BINS) * 4;
+__host__ __device__ constexpr int pk_smem(int nbins) { return (8 * 3 * nbins + 8 * 32 * 4 + nbins) * 4; }
 
 struct RadB { float R, denom; int k2cut, r2max; };   // r2max: sphere painting's largest |d|^2 (-1: none)
 
@@ -84,6 +85,7 @@ struct BatchArgs {
   unsigned* abort;
   long spin_limit;
   int chunk;           // tiles per ticket
+  unsigned long long* prof;   // NULL, or [PROF_OPS][4]: cycles in tiles, tiles, cycles finding and awaiting tickets, tickets
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -92,22 +94,40 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// column tiles: TI columns x N rows; row tiles: RL rows of N/2 complex pairs
-template <int N> struct BCol { static constexpr int TI = 8; };
-template <int N> struct BRow { static constexpr int RL = N >= 128 ? 8 : 16; };
+// Column tiles: TI columns x N rows; row tiles: RL rows of N/2 complex pairs; RS picks the radix
+// schedule (es_fft.cuh Plan<N, RS>).  Chosen so that every stage of the line transforms has
+// close to one butterfly per thread of the CTA or more: a tile's time is its slowest stage's
+// latency, and a radix-16 stage over 8 rows of 80 points keeps only 40 of 256 threads busy.
+template <int N> struct BCol;
+template <> struct BCol<32>  { static constexpr int TI = 16, RS = 0; };
+template <> struct BCol<48>  { static constexpr int TI = 8,  RS = 1; };
+template <> struct BCol<64>  { static constexpr int TI = 16, RS = 1; };
+template <> struct BCol<96>  { static constexpr int TI = 16, RS = 0; };
+template <> struct BCol<128> { static constexpr int TI = 8,  RS = 1; };
+template <> struct BCol<160> { static constexpr int TI = 8,  RS = 0; };
+template <> struct BCol<256> { static constexpr int TI = 8,  RS = 1; };
+template <int N> struct BRow;
+template <> struct BRow<32>  { static constexpr int RL = 32, RS = 1; };
+template <> struct BRow<48>  { static constexpr int RL = 16, RS = 1; };
+template <> struct BRow<64>  { static constexpr int RL = 32, RS = 1; };
+template <> struct BRow<96>  { static constexpr int RL = 16, RS = 1; };
+template <> struct BRow<128> { static constexpr int RL = 16, RS = 1; };
+template <> struct BRow<160> { static constexpr int RL = 16, RS = 1; };
+template <> struct BRow<256> { static constexpr int RL = 8,  RS = 1; };
 
 template <int N> __host__ __device__ constexpr int col_tiles_z() { return N * ((N / 2) / BCol<N>::TI) + N / BCol<N>::TI; }
 template <int N> __host__ __device__ constexpr int col_tiles_y() { return N * ((N / 2) / BCol<N>::TI); }
 template <int N> __host__ __device__ constexpr int row_tiles() { return N * N / BRow<N>::RL; }
 template <int N> __host__ __device__ constexpr int final_tiles() { return (N * N * (N / 2) + FINAL_PAIRS - 1) / FINAL_PAIRS; }
-// column passes: twiddles, two tile buffers (one landing while the other is transformed) and the
+// column passes: twiddles, three tile buffers (two landing while one is transformed) and the
 // transform's second buffer; row passes: twiddles, the transform's two
 // buffers, two raw-row buffers and the previous radius's delta_R tile
-template <int N> __host__ __device__ constexpr int smem_bytes() {
+template <int N> __host__ __device__ constexpr int smem_bytes(int pk_bins) {
   constexpr int TI = BCol<N>::TI, RL = BRow<N>::RL, M = N / 2;
-  constexpr int col = (N + 3 * N * TI) * 8;
+  constexpr int col = (N + 4 * N * TI) * 8;
   constexpr int row = (N + 2 * M * (RL + 1) + 3 * RL * M) * 8;
-  return col > row ? col : row;
+  const int colp = col + (pk_bins ? pk_smem(pk_bins) : 0);   // P(k) bins follow a column tile's buffers
+  return colp > row ? colp : row;
 }
 
 __device__ __forceinline__ void cp16(void* dst, const void* src) {
@@ -116,6 +136,10 @@ __device__ __forceinline__ void cp16(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int K> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory"); }
+__device__ __forceinline__ void cp8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;"
+               ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(__cvta_generic_to_global(src)) : "memory");
+}
 
 __device__ float block_sum_b(float v, float* sred) { return block_sum<BT>(v, sred); }
 
@@ -147,7 +171,8 @@ __device__ __forceinline__ void pk_bin_tile(const BoxDev& b, int plane, int c, b
                                             float* scratch, const int* sthr) {
   constexpr int M = N / 2;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float* wb = bins + warp * PK_MAX_BINS * 3;
+  const int NB = b.nbins;
+  float* wb = bins + warp * NB * 3;
   float* ws = scratch + warp * 32 * 4;
   const float inv = 1.0f / (2.0f * 9.8696044010893586f * b.volume);
   for (int e = threadIdx.x; e < N * TI; e += BT) {       // whole warps iterate together
@@ -176,7 +201,7 @@ __device__ __forceinline__ void pk_bin_tile(const BoxDev& b, int plane, int c, b
         m &= m - 1;
         p += ws[l * 4 + 0]; k += ws[l * 4 + 1]; n += reinterpret_cast<const unsigned*>(ws)[l * 4 + 2];
       }
-      wb[bin] += p; wb[PK_MAX_BINS + bin] += k; reinterpret_cast<unsigned*>(wb)[2 * PK_MAX_BINS + bin] += n;
+      wb[bin] += p; wb[NB + bin] += k; reinterpret_cast<unsigned*>(wb)[2 * NB + bin] += n;
     }
     __syncwarp();
   }
@@ -194,11 +219,11 @@ __device__ __forceinline__ void pk_tile_done(const BoxDev& b, int tile, float* b
     const int q = idx / nb, bin = idx % nb;
     if (q < 2) {
       float acc = 0.f;
-      for (int w = 0; w < 8; ++w) acc += bins[w * PK_MAX_BINS * 3 + q * PK_MAX_BINS + bin];
+      for (int w = 0; w < 8; ++w) acc += bins[w * nb3 + q * nb + bin];
       b.pk_part[(size_t)tile * nb3 + idx] = acc;
     } else {
       unsigned acc = 0u;
-      for (int w = 0; w < 8; ++w) acc += reinterpret_cast<const unsigned*>(bins + w * PK_MAX_BINS * 3)[2 * PK_MAX_BINS + bin];
+      for (int w = 0; w < 8; ++w) acc += reinterpret_cast<const unsigned*>(bins + w * nb3)[2 * nb + bin];
       reinterpret_cast<unsigned*>(b.pk_part)[(size_t)tile * nb3 + idx] = acc;
     }
   }
@@ -244,12 +269,11 @@ __device__ __noinline__ void b_col_chunk(const BoxDev& b, int radius, int t0, in
   constexpr bool Z = OP == B_COL_Z_FWD || OP == B_COL_Z_INV || PK;
   constexpr bool FWD = OP == B_COL_Y_FWD || OP == B_COL_Z_FWD || PK;
   float2* tw = sm;
-  float2* const abuf0 = tw + N;
-  float2* const abuf1 = abuf0 + N * TI;
-  float2* B = abuf1 + N * TI;
-  float* bins = reinterpret_cast<float*>(B + N * TI);          // P(k): [8][3][PK_MAX_BINS]
-  float* scratch = bins + 8 * 3 * PK_MAX_BINS;                  // [8][32][4]
-  int* sthr = reinterpret_cast<int*>(scratch + 8 * 32 * 4);     // [PK_MAX_BINS]
+  float2* const abuf = tw + N;                                 // three tile buffers
+  float2* B = abuf + 3 * N * TI;
+  float* bins = reinterpret_cast<float*>(B + N * TI);          // P(k): [8][3][nbins]
+  float* scratch = bins + 8 * 3 * b.nbins;                      // [8][32][4]
+  int* sthr = reinterpret_cast<int*>(scratch + 8 * 32 * 4);     // [nbins]
   if (PK)
     for (int i = threadIdx.x; i < b.nbins; i += BT) sthr[i] = __ldg(b.thr + i);
   for (int i = threadIdx.x; i < N; i += BT) tw[i] = __ldg(b.tw + i);
@@ -280,38 +304,51 @@ __device__ __noinline__ void b_col_chunk(const BoxDev& b, int radius, int t0, in
     }
     cp_commit();
   };
-  issue(t0, abuf0);
+  // Three tile buffers: two tiles' copies are in flight while one is transformed.  Barriers per
+  // tile: one after the copies land (each thread first fixes up the 16-byte pieces it copied
+  // itself, which cp.async.wait_group makes visible to it) and the transform's own.  Tile t + 2's
+  // copies are issued after that first barrier, when every thread has finished storing tile t - 1
+  // out of the buffer they overwrite.
+  issue(t0, abuf);
+  if (t0 + 1 < t1) issue(t0 + 1, abuf + N * TI);
   for (int tile = t0; tile < t1; ++tile) {
-    float2* A = ((tile - t0) & 1) ? abuf1 : abuf0;
+    float2* A = abuf + ((tile - t0) % 3) * N * TI;
     const bool more = tile + 1 < t1;
-    if (more) issue(tile + 1, ((tile - t0) & 1) ? abuf0 : abuf1);
     const Geo g = geom(tile);
     float2* dst = FWD ? (g.nyq ? b.Xnyq : b.X) : (g.nyq ? Tnyq : T);
     if (PK)
-      for (int i = threadIdx.x; i < 8 * 3 * PK_MAX_BINS; i += BT) bins[i] = 0.f;
-    if (more) cp_wait<1>(); else cp_wait<0>();
-    __syncthreads();
+      for (int i = threadIdx.x; i < 8 * 3 * b.nbins; i += BT) bins[i] = 0.f;
+    if (more) cp_wait<1>(); else cp_wait<0>();          // tile + 1 may stay in flight
     if (OP == B_COL_Z_INV) {
       // W depends on |k|^2 = kz^2 + (the column's ky^2 + kx^2) only: the radius's table row
       const float* wt = b.wtab + (size_t)radius * b.k2n;
-      for (int e = threadIdx.x; e < N * TI; e += BT) {
-        const int row = e / TI, col = e % TI;
-        const int kz = row > M ? N - row : row;
-        const int ck2 = !g.nyq ? wrap2<N>(g.plane) + (g.c * TI + col) * (g.c * TI + col)
-                               : wrap2<N>(g.c * TI + col) + M * M;
-        A[e] = cscale(A[e], __ldg(wt + kz * kz + ck2));
+      for (int q = threadIdx.x; q < N * TI / 2; q += BT) {
+        const int row = q / (TI / 2), col = 2 * (q % (TI / 2));
+        const int kz2 = (row > M ? N - row : row) * (row > M ? N - row : row);
+        int ck0, ck1;
+        if (!g.nyq) {
+          const int w = wrap2<N>(g.plane), kx = g.c * TI + col;
+          ck0 = w + kx * kx; ck1 = w + (kx + 1) * (kx + 1);
+        } else {
+          ck0 = wrap2<N>(g.c * TI + col) + M * M; ck1 = wrap2<N>(g.c * TI + col + 1) + M * M;
+        }
+        float2* a = A + row * TI + col;
+        a[0] = cscale(a[0], __ldg(wt + kz2 + ck0));
+        a[1] = cscale(a[1], __ldg(wt + kz2 + ck1));
       }
-      __syncthreads();
     }
     if (OP == B_COL_Y_INV && g.c == 0) {
-      for (int j = threadIdx.x; j < N; j += BT) {
+      for (int q = threadIdx.x; q < N * TI / 2; q += BT) {
+        if (q % (TI / 2) != 0) continue;                 // the piece holding column 0 of row j
+        const int j = q / (TI / 2);
         const float2 y0 = A[j * TI];
         const float2 ym = __ldcg(Tnyq + (size_t)g.plane * N + j);
         A[j * TI] = make_float2(y0.x - ym.y, y0.y + ym.x);
       }
-      __syncthreads();
     }
-    float2* Rr = fft_lines<N, INV, TI, BT, true, TI, 1, N>(A, B, tw);
+    __syncthreads();
+    if (tile + 2 < t1) issue(tile + 2, abuf + ((tile - t0 + 2) % 3) * N * TI);   // tile - 1's buffer
+    float2* Rr = fft_lines<N, INV, TI, BT, true, TI, 1, N, BCol<N>::RS>(A, B, tw);
     if (PK) {
       pk_bin_tile<N, TI>(b, g.plane, g.c, g.nyq, Rr, bins, scratch, sthr);
       pk_tile_done<N>(b, tile, bins, scratch);
@@ -334,7 +371,7 @@ __device__ __noinline__ void b_col_chunk(const BoxDev& b, int radius, int t0, in
         *reinterpret_cast<float4*>(dst + g.off + row * g.es_g + col) = make_float4(v0.x, v0.y, v1.x, v1.y);
       }
     }
-    __syncthreads();                     // A and B are reused by the next tile
+    if (PK) __syncthreads();             // the bins and scratch are reused by the next tile
   }
 }
 
@@ -364,7 +401,7 @@ __device__ __noinline__ void b_row_r2c(const BoxDev& b, int tile, float2* sm) {
     A[p * ES + row] = v;
   }
   __syncthreads();
-  float2* Z = fft_lines<M, false, RL, BT, true, ES, 1, N>(A, B, tw);
+  float2* Z = fft_lines<M, false, RL, BT, true, ES, 1, N, BRow<N>::RS>(A, B, tw);
   // item t of row l makes X[t] and X[M-t] (item 0: the packed (X[0], X[N/2]) and X[M/2])
   for (int q = threadIdx.x; q < RL * (M / 2); q += BT) {
     const int t = q % (M / 2), l = q / (M / 2);
@@ -410,16 +447,25 @@ __device__ __noinline__ void b_row_c2r_chunk(const BoxDev& b, int radius, int t0
   }
   const float inv_denom = 1.0f / b.rad[radius].denom, dc = b.dc;
   const int lane = threadIdx.x & 31;
+  const f32x2 DC2 = bc2(dc), INV2 = bc2(inv_denom);
   auto issue_rows = [&](const float2* src, size_t pair0, float2* buf) {
     for (int q = threadIdx.x; q < RL * M / 2; q += BT) cp16(buf + 2 * q, src + pair0 + 2 * q);
     cp_commit();
   };
+  // the previous radius's delta_R: each thread copies exactly the pairs its epilogue reads, so
+  // the epilogue needs no barrier after the copies land
+  auto issue_prev = [&](size_t pair0) {
+    for (int e = threadIdx.x; e < RL * M; e += BT) cp8(P + e, prv + pair0 + e);
+    cp_commit();
+  };
+  // Barriers per tile: after the rows land, after the split, the transform's own and one at the
+  // end.  The buffers the next tile's copies overwrite were last read before one of them.
   issue_rows(srcT, (size_t)t0 * RL * M, raw0);
   for (int tile = t0; tile < t1; ++tile) {
     const size_t pair0 = (size_t)tile * RL * M;
     const float2* raw = ((tile - t0) & 1) ? raw1 : raw0;
     const bool more = tile + 1 < t1;
-    if (has_prev) issue_rows(prv, pair0, P); else cp_commit();
+    if (has_prev) issue_prev(pair0); else cp_commit();
     if (more) issue_rows(srcT, pair0 + RL * M, ((tile - t0) & 1) ? raw0 : raw1);
     if (more) cp_wait<2>(); else cp_wait<1>();
     __syncthreads();
@@ -442,14 +488,13 @@ __device__ __noinline__ void b_row_c2r_chunk(const BoxDev& b, int radius, int t0
       }
     }
     __syncthreads();
-    float2* Zr = fft_lines<M, true, RL, BT, true, ES, 1, N>(A, B, tw);
+    float2* Zr = fft_lines<M, true, RL, BT, true, ES, 1, N, BRow<N>::RS>(A, B, tw);
     if (more) cp_wait<1>(); else cp_wait<0>();
-    __syncthreads();
-    float acc = 0.f;
+    f32x2 acc2 = bc2(0.f);
     for (int e = threadIdx.x; e < RL * M; e += BT) {     // whole warps: 64 consecutive voxels
       const int row = e / M, p = e % M;
       const float2 d = Zr[p * ES + row];
-      acc += erfc_sum_term((dc - d.x) * inv_denom) + erfc_sum_term((dc - d.y) * inv_denom);
+      acc2 = add2(acc2, erfc_sum_pair(mul2(sub2(DC2, pk2(d.x, d.y)), INV2)));
       if (has_prev) {
         const float2 pp = P[e];
         const bool px = pp.x >= thr, py = pp.y >= thr;
@@ -470,14 +515,33 @@ __device__ __noinline__ void b_row_c2r_chunk(const BoxDev& b, int radius, int t0
       }
       cur[pair0 + e] = d;
     }
-    float total;
-    if (tile_reduce(acc, b.partials, b.arrive + radius, tile, row_tiles<N>(), sred, &total) && threadIdx.x == 0) {
-      const float mean = total * b.inv_n3;
-      b.stats[4 * radius + 0] = total;
-      b.stats[4 * radius + 1] = mean;
-      b.stats[4 * radius + 2] = b.normalize ? b.fc_mean / mean : 1.f;
-    }
-    __syncthreads();                     // A, B, the raw rows and P are reused by the next tile
+    // the tile's sum as one partial per warp (a fixed lane order), so the radius's total does not
+    // depend on which CTA ran which tiles
+    const float2 a2 = upk2(acc2);
+    float acc = a2.x + a2.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) b.partials[(size_t)tile * (BT / 32) + (threadIdx.x >> 5)] = acc;
+    __syncthreads();                     // ends every thread's reads of A, B, the raw rows and P
+  }
+  // one arrival per ticket; the CTA that completes the pass sums every tile's partials in order
+  __shared__ unsigned s_last;
+  const int tiles = row_tiles<N>();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = (atomicAdd(b.arrive + radius, (unsigned)(t1 - t0)) + (unsigned)(t1 - t0) == (unsigned)tiles) ? 1u : 0u;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  float part = 0.f;
+  for (int i = threadIdx.x; i < tiles * (BT / 32); i += BT) part += __ldcg(b.partials + i);
+  const float total = block_sum_b(part, sred);
+  if (threadIdx.x == 0) {
+    const float mean = total * b.inv_n3;
+    b.stats[4 * radius + 0] = total;
+    b.stats[4 * radius + 1] = mean;
+    b.stats[4 * radius + 2] = b.normalize ? b.fc_mean / mean : 1.f;
   }
 }
 
@@ -509,6 +573,7 @@ __device__ __noinline__ void b_final(const BoxDev& b, int tile, float* sred) {
   const int last = b.n_radii - 1;
   const float2* dR = reinterpret_cast<const float2*>((last & 1) ? b.dR1 : b.dR0);
   const float norm = __ldcg(b.stats + 4 * last + 2), denom = b.rad[last].denom;
+  const f32x2 NORM = bc2(norm), DC = bc2(b.dc), INV = bc2(1.0f / denom);   // as the per-box plans' final step
   const long pairs = (long)N * N * (N / 2);
   const long p0 = (long)tile * FINAL_PAIRS;
   const bool dt = b.tfac != 0.f;
@@ -518,13 +583,11 @@ __device__ __noinline__ void b_final(const BoxDev& b, int tile, float* sred) {
     const unsigned long long w = __ldcg(b.flags + p / 32);
     const int bit = (int)(p % 32);
     float ion[2];
-    const float dv[2] = {d.x, d.y};
+    const float2 f = upk2(mul2(erfc_sum_pair(mul2(sub2(DC, pk2(d.x, d.y)), INV)), NORM));
+    const float fv[2] = {f.x, f.y};
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      if ((w >> (bit + 32 * h)) & 1ull) { ion[h] = 1.0f; continue; }
-      const float f = erfcf((b.dc - dv[h]) / denom) * norm;
-      ion[h] = f >= b.inv_zeta ? 1.0f : f * b.zeta;
-    }
+    for (int h = 0; h < 2; ++h)
+      ion[h] = ((w >> (bit + 32 * h)) & 1ull) ? 1.0f : (fv[h] >= b.inv_zeta ? 1.0f : fv[h] * b.zeta);
     acc += (1.0f - ion[0]) + (1.0f - ion[1]);
     reinterpret_cast<float2*>(b.out)[p] =
         b.output == 0 ? make_float2(1.0f - ion[0], 1.0f - ion[1]) : make_float2(ion[0], ion[1]);
@@ -589,6 +652,7 @@ __global__ void __launch_bounds__(BT, 4) batch_kernel(BatchArgs g) {
   for (;;) {
     const unsigned t = s_t;
     if (t >= g.total) break;
+    const long long c_start = clock64();
     if (threadIdx.x < 32) {
       // the next ticket is taken now, so its latency hides behind this one's work; tickets only
       // grow, so the pass holding t is at or after the previous ticket's (32-ary search)
@@ -624,6 +688,7 @@ __global__ void __launch_bounds__(BT, 4) batch_kernel(BatchArgs g) {
       }
     }
     __syncthreads();
+    const long long c_ready = clock64();
     if (!s_go) break;
     const PassDesc pd = g.passes[s_pass];
     const BoxDev& b = g.boxes[pd.box];
@@ -637,6 +702,13 @@ __global__ void __launch_bounds__(BT, 4) batch_kernel(BatchArgs g) {
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
+      if (g.prof) {                                      // SM clock cycles of this CTA
+        unsigned long long* c = g.prof + 4 * pd.op;
+        atomicAdd(c + 0, (unsigned long long)(clock64() - c_ready));
+        atomicAdd(c + 1, (unsigned long long)(t1 - t0));
+        atomicAdd(c + 2, (unsigned long long)(c_ready - c_start));
+        atomicAdd(c + 3, 1ull);
+      }
       atomicAdd(g.done + s_pass, 1u);
       s_t = *(volatile unsigned*)g.abort ? g.total : s_next;
     }
@@ -670,18 +742,18 @@ int bfail(int code, const char* fmt, ...) {
 size_t a256(size_t x) { return (x + 255) / 256 * 256; }
 
 template <int N> struct SizeInfo {
-  static void get(int* ct_z, int* ct_y, int* rt, int* ft, int* smem) {
+  static void get(int* ct_z, int* ct_y, int* rt, int* ft, int* smem, int pk_bins) {
     *ct_z = esb::col_tiles_z<N>();
     *ct_y = esb::col_tiles_y<N>();
     *rt = esb::row_tiles<N>();
     *ft = esb::final_tiles<N>();
-    *smem = esb::smem_bytes<N>();
+    *smem = esb::smem_bytes<N>(pk_bins);
   }
 };
 
-bool size_info(int n, int* ct_z, int* ct_y, int* rt, int* ft, int* smem) {
+bool size_info(int n, int* ct_z, int* ct_y, int* rt, int* ft, int* smem, int pk_bins = 0) {
   switch (n) {
-#define ESB_INFO(NN) case NN: SizeInfo<NN>::get(ct_z, ct_y, rt, ft, smem); return true;
+#define ESB_INFO(NN) case NN: SizeInfo<NN>::get(ct_z, ct_y, rt, ft, smem, pk_bins); return true;
     ESB_SIZES(ESB_INFO)
 #undef ESB_INFO
     default: return false;
@@ -704,6 +776,7 @@ struct es_batch {
   cudaGraphExec_t graph = nullptr;
   long spin_limit = esb::kSpinLimit;
   int lanes = 0, chunk = 1;          // queue schedule (lanes 0: every box its own lane)
+  unsigned long long* prof = nullptr;  // per-op cycle counters while profiling
   std::vector<esb::PassDesc> h_passes;
   std::vector<std::vector<esb::PassDesc>> per_box;   // dep / dep2: indices within the box's list
   std::vector<int> h_n, h_nr;                        // HII_DIM and radius count per box
@@ -773,7 +846,12 @@ unsigned make_queue(const std::vector<PassList>& per_box, const std::vector<int>
     lane_boxes[best].push_back(i);
     load[best] += cost[i];
   }
-  // lanes advance in proportion to work: always extend the lane with the least work queued
+  // lanes advance in proportion to their own total work (passes x N^3), so they all finish together
+  // and the end of the queue still holds many independent passes: always extend the lane that
+  // has queued the smallest fraction of its work
+  std::vector<double> lane_work(L, 0.0);
+  for (int l = 0; l < L; ++l)
+    for (int i : lane_boxes[l]) lane_work[l] += (double)per_box[i].size() * std::pow((double)n[i], 3);
   struct Cursor { size_t box = 0, pass = 0; double work = 0.0; };
   std::vector<Cursor> cur(L);
   std::vector<std::vector<int>> gidx(count);
@@ -799,7 +877,7 @@ unsigned make_queue(const std::vector<PassList>& per_box, const std::vector<int>
     first += (unsigned)d.tickets;
     gidx[box][c.pass] = (int)q.size();
     q.push_back(d);
-    c.work += std::pow((double)n[box], 3);
+    c.work += std::pow((double)n[box], 3) / lane_work[pick];
     if (++c.pass == per_box[box].size()) { c.pass = 0; ++c.box; }
   }
   return first;
@@ -858,13 +936,13 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
         if (bx.k2_thresholds[k] < bx.k2_thresholds[k - 1])
           return cleanup(bfail(ES_E_ARG, "es_batch_create: box %d: k^2 thresholds must be non-decreasing", i));
     }
-    if (want_pk) sm += esb::PK_SMEM;
+    if (want_pk) size_info(bx.n, &ctz, &cty, &rt, &ft, &sm, bx.nbins);
     smem = sm > smem ? sm : smem;
     const size_t N = bx.n, M = N / 2;
     Sz& s = sz[i];
     s.X = a256(N * N * M * 8); s.Xn = a256(N * N * 8); s.T = 2 * s.X; s.Tn = 2 * s.Xn;
     s.dR = a256(N * N * N * 4); s.flags = a256(N * N * N / 8); s.stats = a256((size_t)p.n_radii * 16);
-    s.partials = a256((size_t)(rt > ft ? rt : ft) * 4); s.arrive = a256((size_t)(p.n_radii + 3) * 4);
+    s.partials = a256((size_t)(rt * (esb::BT / 32) > ft ? rt * (esb::BT / 32) : ft) * 4); s.arrive = a256((size_t)(p.n_radii + 3) * 4);
     s.rad = a256((size_t)p.n_radii * sizeof(esb::RadB)); s.tw = a256(N * 8);
     s.wtab = a256((size_t)p.n_radii * (3 * M * M + 1) * 4);
     s.centers = p.update ? a256(N * N * N * 4) : 0;
@@ -884,7 +962,7 @@ int es_batch_create(const es_batch_box* boxes, int count, es_batch** out) {
     bt->per_box[i] = box_passes(i, boxes[i].n, boxes[i].params.n_radii, boxes[i].params.update,
                                 boxes[i].t_factor != 0.f && boxes[i].k2_thresholds ? 1 : 0);
   }
-  build_queue(bt, 0, 8);
+  build_queue(bt, 0, 16);
   bt->npasses = (int)bt->h_passes.size();
   bt->smem = smem;
   const size_t ctrl_bytes = a256((3 + bt->h_passes.size()) * 4);
@@ -1021,6 +1099,7 @@ static int batch_enqueue(es_batch* bt, cudaStream_t s) {
   g.done = bt->ctrl + 3;
   g.spin_limit = bt->spin_limit;
   g.chunk = bt->chunk;
+  g.prof = bt->prof;
   esb::batch_kernel<<<bt->grid, esb::BT, bt->smem, s>>>(g);
   ESB_CUDA(cudaGetLastError());
   return ES_OK;
@@ -1095,6 +1174,29 @@ int es_batch_set_schedule(es_batch* bt, int lanes, int chunk) {
   return ES_OK;
 }
 
+int es_batch_profile(es_batch* bt, int enable) {
+  if (!bt) return bfail(ES_E_ARG, "es_batch_profile: NULL batch");
+  const size_t bytes = sizeof(unsigned long long) * esb::PROF_OPS * 4;
+  if (enable) {
+    if (!bt->prof) ESB_CUDA(cudaMalloc(&bt->prof, bytes));
+    ESB_CUDA(cudaMemset(bt->prof, 0, bytes));
+  } else if (bt->prof) {
+    cudaFree(bt->prof);
+    bt->prof = nullptr;
+  }
+  if (bt->graph) { cudaGraphExecDestroy(bt->graph); bt->graph = nullptr; }
+  return ES_OK;
+}
+
+int es_batch_profile_read(es_batch* bt, unsigned long long* out, int nops) {
+  if (!bt || !out || nops < 1) return bfail(ES_E_ARG, "es_batch_profile_read: bad arguments");
+  if (!bt->prof) return bfail(ES_E_ARG, "es_batch_profile_read: profiling is off");
+  const int n = nops < esb::PROF_OPS ? nops : esb::PROF_OPS;
+  ESB_CUDA(cudaDeviceSynchronize());
+  ESB_CUDA(cudaMemcpy(out, bt->prof, sizeof(unsigned long long) * 4 * n, cudaMemcpyDeviceToHost));
+  return ES_OK;
+}
+
 int es_batch_get_schedule(const es_batch* bt, int* lanes, int* chunk, unsigned* tickets) {
   if (!bt) return bfail(ES_E_ARG, "es_batch_get_schedule: NULL batch");
   if (lanes) *lanes = bt->lanes;
@@ -1129,6 +1231,7 @@ int es_batch_destroy(es_batch* bt) {
   if (!bt) return ES_OK;
   if (bt->graph) cudaGraphExecDestroy(bt->graph);
   if (bt->base) cudaFree(bt->base);
+  if (bt->prof) cudaFree(bt->prof);
   delete bt;
   return ES_OK;
 }

@@ -770,6 +770,7 @@ def run_batch(args, dev):
     boxes = batch.boxes_from_specs(specs, dev)
     stream = torch.cuda.current_stream(dev)
     b = batch.BatchedExcursionSet(boxes, use_graph=True, device=dev)
+    sched_ms = at.tune_batch(b, schedules=[(0, 8), (0, 16), (32, 8)], repeats=2)
     for _ in range(3):
         b.run()
     b.check()
@@ -783,6 +784,14 @@ def run_batch(args, dev):
     t_batch = e0.elapsed_time(e1) / 1e3 / args.steps
     updates = b.voxel_radius_updates()
     info = b.info()
+    # where the persistent launch's CTA time goes, per pass kind (one extra launch, counters on)
+    b.profile(True)
+    b.run()
+    prof = b.profile_read()
+    b.profile(False)
+    total_cyc = sum(v["tile_cycles"] + v["wait_cycles"] for v in prof.values())
+    op_share = {k: round((v["tile_cycles"] + v["wait_cycles"]) / total_cyc, 4) for k, v in prof.items()}
+    cyc_per_tile = {k: round(v["tile_cycles"] / v["tiles"]) for k, v in prof.items()}
     b.close()
     plans = {}
     for d, st in boxes:
@@ -824,10 +833,13 @@ def run_batch(args, dev):
                         "R_mfp ~ U[5,50] Mpc, log10 Tvir ~ U[4,5.3], z ~ U[6,10]; x_HI of every box",
             "value": modes[best], "mode": best, "unit": UNIT,
             "persistent_value": modes["persistent"], "persistent_ms_per_batch": 1e3 * t_batch,
+            "persistent_schedule": {"lanes": info["lanes"], "tiles_per_ticket": info["chunk"],
+                                    "tuned_ms": {f"{k[0]}x{k[1]}": round(v, 3) for k, v in sched_ms.items()}},
+            "persistent_op_share": op_share, "persistent_cycles_per_tile": cyc_per_tile,
             "plan_graph_value": modes["plan_graph"], "plan_graph_ms_per_batch": 1e3 * t_graph,
             "per_box_plans_value": updates / t_loop, "per_box_plans_ms": 1e3 * t_loop,
             "launch": f"persistent: one launch per batch ({info['grid']} CTAs, {info['passes']} passes, "
-                      f"{info['tiles']} tiles) replayed from a CUDA graph; plan_graph: {ginfo['lanes']} "
+                      f"{info['tiles']} tiles in {info['tickets']} tickets) replayed from a CUDA graph; plan_graph: {ginfo['lanes']} "
                       "autotuned plans on their own streams (two per box size, overlapped radii), the "
                       "whole batch captured in one CUDA graph; per_box_plans: one plan per size, boxes in turn"}
 

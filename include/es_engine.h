@@ -212,9 +212,16 @@ int es_batch_run(es_batch* batch, int use_graph, void* stream);
 int es_batch_check(es_batch* batch, void* stream);
 int es_batch_info(const es_batch* batch, int* grid, int* passes, unsigned* tiles, int* smem);
 /* Queue schedule: `lanes` boxes in flight (0 = every box its own lane, the default), `chunk`
- * tiles per ticket (1..64, default 8).  Rebuilds the queue; the next es_batch_run recaptures. */
+ * tiles per ticket (1..64, default 16).  Rebuilds the queue; the next es_batch_run recaptures. */
 int es_batch_set_schedule(es_batch* batch, int lanes, int chunk);
 int es_batch_get_schedule(const es_batch* batch, int* lanes, int* chunk, unsigned* tickets);
+/* Per-op profile of the persistent launch: es_batch_profile(batch, 1) clears and enables
+ * counters that every launch afterwards adds to (0 frees them); es_batch_profile_read
+ * synchronises the device and writes, per op code (as es_batch_queue's, nops <= 16), four
+ * counts: SM clock cycles CTAs spent in the op's tiles, tiles, cycles finding and awaiting the
+ * op's tickets, tickets. */
+int es_batch_profile(es_batch* batch, int enable);
+int es_batch_profile_read(es_batch* batch, unsigned long long* out, int nops);
 /* The work queue es_batch_create would build for boxes of HII_DIM n[i] with n_radii[i] radii and
  * update mode update[i] (NULL: all 0) under a schedule, computed on the host (no device needed):
  * per pass 8 ints (box, op, radius, tiles, first ticket, tickets, dependency, second dependency;

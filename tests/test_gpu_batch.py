@@ -141,6 +141,23 @@ def test_batch_delta_T_and_pk_match_per_box_plans(mods):
     compare_pk(pk[1], O.power_spectrum(dT_o, ave_o, st.box_len, edges[1]), "batch P(k)")
 
 
+def test_batch_profile_counts_every_tile(mods):
+    _, batch = mods
+    boxes = _boxes(SPECS[:3])
+    with batch.BatchedExcursionSet(boxes, use_graph=True, chunk=4) as b:
+        b.profile(True)
+        b.run()
+        b.run()
+        prof = b.profile_read()
+        b.profile(False)
+        b.check()
+    q = batch.queue_plan([st.n for _, st in boxes], [st.n_radii for _, st in boxes], 0, 4)
+    for op in ("z_inv", "y_inv", "row_c2r", "final", "wtab"):
+        assert prof[op]["tiles"] == 2 * sum(d["tiles"] for d in q if d["op"] == op), op
+        assert prof[op]["tickets"] == 2 * sum(d["tickets"] for d in q if d["op"] == op), op
+        assert prof[op]["tile_cycles"] > 0
+
+
 def test_batch_graph_replay_is_deterministic(mods):
     _, batch = mods
     boxes = _boxes(SPECS[:4])
