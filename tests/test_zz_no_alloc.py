@@ -31,12 +31,12 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
-def test_noalloc_delta_T_matches_plan_entry_point_twice(lib):
+@pytest.mark.parametrize("n", [64, 256])     # 256^3: every CTA's grid-stride loop runs many times
+def test_noalloc_delta_T_matches_plan_entry_point_twice(lib, n):
     _lib = module("_lib")
     eng = module("engine")
-    n = 64
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    with eng.ExcursionSetPlan(n, 100.0) as plan:
+    with eng.ExcursionSetPlan(n, 1.5 * n) as plan:
         for call, seed in enumerate((1, 2)):           # two calls in a row, different inputs
             g = torch.Generator(device="cuda").manual_seed(seed)
             xH = torch.rand((n, n, n), device="cuda", generator=g)
