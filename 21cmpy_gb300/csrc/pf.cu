@@ -14,7 +14,7 @@
 // DIM index are computed on the host (in double and in float32 respectively, as the reference's
 // device code does) and passed as tables, so the device arithmetic is FP32 only.
 //
-// The scatter runs a grid-stride loop of warps over bricks of 1 x 4 x 8 cells with one 64-bit
+// The scatter runs a grid-stride loop of warps over bricks of 4 x 4 x 8 cells with one 64-bit
 // integer atomic per cell; the accumulator (8 bytes per HII cell) stays in L2.
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -52,37 +52,66 @@ __device__ __forceinline__ int target(float p, float vel, float ds, float swf, i
   return i < 0 ? 0 : (i >= sw ? sw - 1 : i);
 }
 
-// Warps walk bricks of 1 x 4 x 8 cells (axes 0, 1, 2), every 8 lanes reading 32 contiguous bytes
-// of deltax; a lane adds its cell's mass with one 64-bit atomic (the accumulator is L2-resident and
-// the atomics overlap the rest: merging equal targets inside the warp, or summing a lane's cells
-// along axis 0 in registers first, both measured slower).  The brick index advances by the grid's
-// warp count as a mixed-radix (axis 0, 1, 2) counter, so the loop needs no integer division.
+// Warps walk bricks of 4 x 4 x 8 cells (axes 0, 1, 2): a lane owns a run of 4 cells along axis 0
+// at one (a1, a2), and every 8 lanes read 32 contiguous bytes of deltax per cell of the run.  The
+// run's cells share a1 and a2, so their axis-1 and axis-2 positions, and while they stay in one
+// HII cell also the displacement gathers and the axis-1 / axis-2 targets, are computed once per
+// run (the HII cell along axis 0 is the same for the whole warp, so the test does not diverge).
+// Consecutive cells of a run that land in the same cell add their fixed-point masses in a register
+// first; each group then takes one 64-bit atomic (the accumulator is L2-resident).  The brick
+// index advances by the grid's warp count as a mixed-radix (axis 0, 1, 2) counter, so the loop
+// needs no integer division.
+constexpr int kRun = 4;                         // cells per lane along axis 0
 __global__ void __launch_bounds__(256) move_mass_kernel(int dim, int sw, const float* __restrict__ delta,
                                                         const float* __restrict__ vx, const float* __restrict__ vy,
                                                         const float* __restrict__ vz, const float* __restrict__ pos,
                                                         const int* __restrict__ hidx, float g0, float ds,
                                                         unsigned long long* __restrict__ acc) {
-  const int nb1 = (dim + 3) / 4, nb2 = (dim + 7) / 8;
+  const int nb0 = (dim + kRun - 1) / kRun, nb1 = (dim + 3) / 4, nb2 = (dim + 7) / 8;
   const int warps = (int)(gridDim.x * (blockDim.x / 32));
   const int w2 = warps % nb2, w1 = (warps / nb2) % nb1, w0 = warps / (nb2 * nb1);
   const int id = (int)(blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5));
   int c2 = id % nb2, c1 = (id / nb2) % nb1, c0 = id / (nb2 * nb1);
   const float swf = (float)sw;
+  const unsigned usw = (unsigned)sw;
   const int lane = threadIdx.x & 31;
   const int l1 = lane >> 3, l2 = lane & 7;
-  while (c0 < dim) {
-    const int a0 = c0, a1 = c1 * 4 + l1, a2 = c2 * 8 + l2;
+  while (c0 < nb0) {
+    const int a1 = c1 * 4 + l1, a2 = c2 * 8 + l2;
     if (a1 < dim && a2 < dim) {
-      // HII grids up to 1024^3 index in 32 bits; deltax rows are addressed from a 64-bit base
-      const unsigned sc = ((unsigned)hidx[a0] * (unsigned)sw + (unsigned)hidx[a1]) * (unsigned)sw + (unsigned)hidx[a2];
-      const int t0 = target(pos[a0], __ldg(vx + sc), ds, swf, sw);
-      const int t1 = target(pos[a1], __ldg(vy + sc), ds, swf, sw);
-      const int t2 = target(pos[a2], __ldg(vz + sc), ds, swf, sw);
-      const float* row = delta + ((size_t)a0 * dim + a1) * dim;
-      const float mass = __fadd_rn(1.0f, __fmul_rn(g0, __ldg(row + a2)));
-      const long long q = __float2ll_rn(mass * kFix);   // exact scaling by a power of two, then rounding
-      atomicAdd(acc + (((unsigned)t0 * (unsigned)sw + (unsigned)t1) * (unsigned)sw + (unsigned)t2),
-                (unsigned long long)q);
+      const unsigned h1 = (unsigned)__ldg(hidx + a1), h2 = (unsigned)__ldg(hidx + a2);
+      const float p1 = __ldg(pos + a1), p2 = __ldg(pos + a2);
+      int hprev = -1, t1 = 0, t2 = 0;
+      float vxv = 0.0f;
+      unsigned run_t = 0xffffffffu;              // the run's cells that land in one cell add up first
+      unsigned long long run_q = 0ull;
+#pragma unroll
+      for (int k = 0; k < kRun; ++k) {
+        const int a0 = c0 * kRun + k;
+        if (a0 < dim) {
+          const int h0 = __ldg(hidx + a0);
+          if (h0 != hprev) {
+            // HII grids up to 1024^3 index in 32 bits
+            const unsigned sc = ((unsigned)h0 * usw + h1) * usw + h2;
+            vxv = __ldg(vx + sc);
+            t1 = target(p1, __ldg(vy + sc), ds, swf, sw);
+            t2 = target(p2, __ldg(vz + sc), ds, swf, sw);
+            hprev = h0;
+          }
+          const int t0 = target(__ldg(pos + a0), vxv, ds, swf, sw);
+          const float* row = delta + ((size_t)a0 * dim + a1) * dim;   // 64-bit row base
+          const float mass = __fadd_rn(1.0f, __fmul_rn(g0, __ldg(row + a2)));
+          const long long q = __float2ll_rn(mass * kFix);   // exact scaling by a power of two, then rounding
+          const unsigned t = ((unsigned)t0 * usw + (unsigned)t1) * usw + (unsigned)t2;
+          if (t != run_t) {                      // integer sums: the grouping does not change the result
+            if (run_t != 0xffffffffu) atomicAdd(acc + run_t, run_q);
+            run_t = t;
+            run_q = 0ull;
+          }
+          run_q += (unsigned long long)q;
+        }
+      }
+      if (run_t != 0xffffffffu) atomicAdd(acc + run_t, run_q);
     }
     c2 += w2;
     if (c2 >= nb2) { c2 -= nb2; ++c1; }
@@ -193,7 +222,7 @@ int pf_move_mass(pf_plan* p, const float* delta, const float* vx, const float* v
   cudaStream_t s = (cudaStream_t)stream;
   const long cells = (long)p->hii * p->hii * p->hii;
   PF_CUDA(cudaMemsetAsync(p->acc, 0, cells * sizeof(unsigned long long), s));
-  const long bricks = (long)p->dim * ((p->dim + 3) / 4) * ((p->dim + 7) / 8);
+  const long bricks = (long)((p->dim + pf::kRun - 1) / pf::kRun) * ((p->dim + 3) / 4) * ((p->dim + 7) / 8);
   long blocks = (bricks + 7) / 8;                 // 8 warps per block
   const long cap = (long)p->sms * 8;
   if (blocks > cap) blocks = cap;
