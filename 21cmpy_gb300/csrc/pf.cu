@@ -14,8 +14,9 @@
 // DIM index are computed on the host (in double and in float32 respectively, as the reference's
 // device code does) and passed as tables, so the device arithmetic is FP32 only.
 //
-// The scatter runs a grid-stride loop of warps over bricks of 4 x 4 x 8 cells with one 64-bit
-// integer atomic per cell; the accumulator (8 bytes per HII cell) stays in L2.
+// The scatter runs a grid-stride loop of warps over bricks of 8 x 4 x 8 cells; cells of a lane's
+// run that land in one cell share a 64-bit integer atomic; the accumulator (8 bytes per HII cell)
+// stays in L2.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -52,7 +53,7 @@ __device__ __forceinline__ int target(float p, float vel, float ds, float swf, i
   return i < 0 ? 0 : (i >= sw ? sw - 1 : i);
 }
 
-// Warps walk bricks of 4 x 4 x 8 cells (axes 0, 1, 2): a lane owns a run of 4 cells along axis 0
+// Warps walk bricks of 8 x 4 x 8 cells (axes 0, 1, 2): a lane owns a run of 8 cells along axis 0
 // at one (a1, a2), and every 8 lanes read 32 contiguous bytes of deltax per cell of the run.  The
 // run's cells share a1 and a2, so their axis-1 and axis-2 positions, and while they stay in one
 // HII cell also the displacement gathers and the axis-1 / axis-2 targets, are computed once per
@@ -61,7 +62,7 @@ __device__ __forceinline__ int target(float p, float vel, float ds, float swf, i
 // first; each group then takes one 64-bit atomic (the accumulator is L2-resident).  The brick
 // index advances by the grid's warp count as a mixed-radix (axis 0, 1, 2) counter, so the loop
 // needs no integer division.
-constexpr int kRun = 4;                         // cells per lane along axis 0
+constexpr int kRun = 8;                         // cells per lane along axis 0
 __global__ void __launch_bounds__(256) move_mass_kernel(int dim, int sw, const float* __restrict__ delta,
                                                         const float* __restrict__ vx, const float* __restrict__ vy,
                                                         const float* __restrict__ vz, const float* __restrict__ pos,
