@@ -1,7 +1,7 @@
 """Train and evaluate the learned surrogate on pairs generated by the plain engine.
 
     python -m 21cmpy_gb300.Programs.train_surrogate [--n 128] [--box-len 200] [--train 2048]
-        [--held 128] [--epochs 30] [--lr 3e-4] [--decay 0.9] [--out weights.pt] [--report report.json]
+        [--held 128] [--epochs 60] [--lr 3e-4] [--decay 0.95] [--out weights.pt] [--report report.json]
     python -m 21cmpy_gb300.Programs.train_surrogate --conv-only [--n 128]
 
 Training pairs: Gaussian random fields of seeds 1000..(1000 + train - 1) at n^3 with parameter
@@ -30,9 +30,9 @@ def main(argv=None):
     ap.add_argument("--box-len", type=float, default=200.0)
     ap.add_argument("--train", type=int, default=2048)
     ap.add_argument("--held", type=int, default=128)
-    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--lr", type=float, default=3e-4)
-    ap.add_argument("--decay", type=float, default=0.9, help="step-size factor per epoch")
+    ap.add_argument("--decay", type=float, default=0.95, help="step-size factor per epoch")
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--smooth", default=",".join(f"{r:g}" for r in S.SMOOTH_CELLS),
                     help="radii (cells) of the smoothed input channels, comma-separated; empty for none")
