@@ -3,8 +3,8 @@
 No counterpart in the reference.  An 8-layer 3D convolutional network (3^3 kernels, circular
 padding, 32 hidden channels, ReLU, sigmoid output) whose forward and backward passes run on the
 project's BF16 tensor-core kernels (``sg_conv3d_fwd`` / ``sg_conv3d_wgrad``, FP32 accumulation).
-Training pairs come from the plain engine; the plain engine is also the judge of the surrogate's
-error and its fallback (:class:`SurrogateSweep`).
+Training pairs come from the plain engine; the plain engine also measures the surrogate's error
+and is its fallback (:class:`SurrogateSweep`).
 
 Channels-last BF16 activations [n][n][n][C].  Input features (16 channels, 5 + len(smoothing)
 used): normalised density delta / (4 D(z)), zeta / 80, R_mfp / 50, log10(T_vir) - 4, (z - 6) / 4,
