@@ -358,16 +358,23 @@ __device__ __forceinline__ void pk_finish(float* bins, const OpArgs& a) {
   __syncthreads();
   if (!s_last) return;
   __threadfence();
+  // One warp per value: lanes stride over the CTAs' partials (32 loads in flight instead of one
+  // dependent chain per thread), then a fixed butterfly: deterministic
   float* tot = bins;                                  // reuse: [3 * nbins]
-  for (int idx = threadIdx.x; idx < nb3; idx += T) {
+  const int lane = threadIdx.x & 31;
+  for (int idx = threadIdx.x >> 5; idx < nb3; idx += T / 32) {
     if (idx < 2 * a.nbins) {
       float s = 0.f;
-      for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(a.partials + (size_t)b * nb3 + idx);
-      tot[idx] = s;
+      for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(a.partials + (size_t)b * nb3 + idx);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) tot[idx] = s;
     } else {
       unsigned long long s = 0ull;
-      for (int b = 0; b < (int)gridDim.x; ++b) s += __float_as_uint(__ldcg(a.partials + (size_t)b * nb3 + idx));
-      tot[idx] = __ull2float_rn(s);
+      for (int b = lane; b < (int)gridDim.x; b += 32) s += __float_as_uint(__ldcg(a.partials + (size_t)b * nb3 + idx));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) tot[idx] = __ull2float_rn(s);
     }
   }
   __syncthreads();

@@ -220,7 +220,7 @@ template <int N, int MODE, int V> struct TmaSmem {
   static constexpr int TI = ColTile<N, V>::TI, T = ColTile<N, V>::T;
   static constexpr int tile = N * TI * 8;
   static constexpr int pk = (MODE == COL_Z_FWD_PK)
-      ? ((T / 32) * PK_MAX_BINS * 3 + (T / 32) * 32 * 4 + PK_MAX_BINS) * 4
+      ? ((T / 32) * PK_MAX_BINS * 3 + PK_MAX_BINS) * 4
       : (MODE == COL_Z_INV_FILTER ? TI * (N / 2 + 1) * 4 : 0);    // per-tile filter weights
   // [S0 | S1 | W | twiddles | pk bins or filter weights | 2 mbarriers] after aligning the base
   static constexpr int bytes = 3 * tile + N * 8 + pk + 16 + 128;
@@ -245,8 +245,7 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
   float2* tw = W + N * TI;
   float* bins = reinterpret_cast<float*>(tw + N);
   float* wcol = bins;                         // COL_Z_INV_FILTER: W[col][|kz|], TI x (N/2 + 1)
-  float* scratch = bins + (T / 32) * PK_MAX_BINS * 3;
-  int* sthr = reinterpret_cast<int*>(scratch + (T / 32) * 32 * 4);
+  int* sthr = reinterpret_cast<int*>(bins + (T / 32) * PK_MAX_BINS * 3);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + 3 * TmaSmem<N, MODE, V>::tile + N * 8 + TmaSmem<N, MODE, V>::pk);
   __shared__ int s_abort;
 
@@ -336,7 +335,10 @@ __global__ void __launch_bounds__(ColTile<N, V>::T, ColTile<N, V>::MINB) col_tma
       static_assert(NSEG * TI == T, "threads must cover whole columns");
       const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
       float* wb = bins + warp * PK_MAX_BINS * 3;
-      float* ws = scratch + warp * 32 * 4;
+      // the warps' merge scratch [warps][32][4] lives in whichever of S / W the transform left free
+      // (this tile's input buffer is loaded again only after the barrier that ends the tile), so
+      // the P(k) pass needs no shared memory of its own beyond the bins and fits two CTAs per SM
+      float* ws = reinterpret_cast<float*>(out == W ? S : W) + warp * 32 * 4;
       const float inv = 1.0f / (2.0f * 9.8696044010893586f * a.volume);
       const int col = threadIdx.x % TI, k0 = (threadIdx.x / TI) * KR;
       int ck2;
