@@ -495,14 +495,25 @@ __device__ __noinline__ void b_row_c2r_chunk(const BoxDev& b, int radius, int t0
       const int row = e / M, p = e % M;
       const float2 d = Zr[p * ES + row];
       acc2 = add2(acc2, erfc_sum_pair(mul2(sub2(DC2, pk2(d.x, d.y)), INV2)));
+      if (!b.update) {
+        // centre mode: a cell's "ionised by an earlier radius" flag rides in the lowest mantissa
+        // bit of its delta_R (as in the per-box plans): the previous radius's bit, or its test
+        unsigned fx = 0u, fy = 0u;
+        if (has_prev) {
+          const float2 pp = P[e];
+          fx = (__float_as_uint(pp.x) & 1u) | (pp.x >= thr ? 1u : 0u);
+          fy = (__float_as_uint(pp.y) & 1u) | (pp.y >= thr ? 1u : 0u);
+        }
+        cur[pair0 + e] = make_float2(__uint_as_float((__float_as_uint(d.x) & ~1u) | fx),
+                                     __uint_as_float((__float_as_uint(d.y) & ~1u) | fy));
+        continue;
+      }
       if (has_prev) {
         const float2 pp = P[e];
         const bool px = pp.x >= thr, py = pp.y >= thr;
         const unsigned bx = __ballot_sync(0xffffffffu, px);
         const unsigned by = __ballot_sync(0xffffffffu, py);
-        if (!b.update) {
-          if (lane == 0 && (bx | by)) atomicOr(b.flags + (pair0 + e) / 32, ((unsigned long long)by << 32) | bx);
-        } else if (bx | by) {              // sphere mode: list the centres for the painting pass
+        if (bx | by) {                     // sphere mode: list the centres for the painting pass
           unsigned first = 0;
           if (lane == 0) first = atomicAdd(b.ccount + radius, __popc(bx) + __popc(by));
           first = __shfl_sync(0xffffffffu, first, 0);
@@ -580,14 +591,22 @@ __device__ __noinline__ void b_final(const BoxDev& b, int tile, float* sred) {
   float acc = 0.f, acc_t = 0.f;
   for (long p = p0 + threadIdx.x; p < p0 + FINAL_PAIRS && p < pairs; p += BT) {
     const float2 d = __ldcg(dR + p);
-    const unsigned long long w = __ldcg(b.flags + p / 32);
-    const int bit = (int)(p % 32);
+    unsigned fl[2];
+    if (!b.update) {                                   // centre mode: the flag in delta_R's lowest bit
+      fl[0] = __float_as_uint(d.x) & 1u;
+      fl[1] = __float_as_uint(d.y) & 1u;
+    } else {                                           // sphere mode: the painted bitmap
+      const unsigned long long w = __ldcg(b.flags + p / 32);
+      const int bit = (int)(p % 32);
+      fl[0] = (unsigned)(w >> bit) & 1u;
+      fl[1] = (unsigned)(w >> (bit + 32)) & 1u;
+    }
     float ion[2];
     const float2 f = upk2(mul2(erfc_sum_pair(mul2(sub2(DC, pk2(d.x, d.y)), INV)), NORM));
     const float fv[2] = {f.x, f.y};
 #pragma unroll
     for (int h = 0; h < 2; ++h)
-      ion[h] = ((w >> (bit + 32 * h)) & 1ull) ? 1.0f : (fv[h] >= b.inv_zeta ? 1.0f : fv[h] * b.zeta);
+      ion[h] = fl[h] ? 1.0f : (fv[h] >= b.inv_zeta ? 1.0f : fv[h] * b.zeta);
     acc += (1.0f - ion[0]) + (1.0f - ion[1]);
     reinterpret_cast<float2*>(b.out)[p] =
         b.output == 0 ? make_float2(1.0f - ion[0], 1.0f - ion[1]) : make_float2(ion[0], ion[1]);
