@@ -212,7 +212,8 @@ int es_batch_run(es_batch* batch, int use_graph, void* stream);
 int es_batch_check(es_batch* batch, void* stream);
 int es_batch_info(const es_batch* batch, int* grid, int* passes, unsigned* tiles, int* smem);
 /* Queue schedule: `lanes` boxes in flight (0 = every box its own lane, the default), `chunk`
- * tiles per ticket (1..64, default 16).  Rebuilds the queue; the next es_batch_run recaptures. */
+ * tiles per ticket (1..64; by default 16, 8 or 4 as the batch gives each resident CTA at least
+ * 4000, 1000 or fewer tiles).  Rebuilds the queue; the next es_batch_run recaptures. */
 int es_batch_set_schedule(es_batch* batch, int lanes, int chunk);
 int es_batch_get_schedule(const es_batch* batch, int* lanes, int* chunk, unsigned* tickets);
 /* Per-op profile of the persistent launch: es_batch_profile(batch, 1) clears and enables
